@@ -1,0 +1,264 @@
+/*
+ * eleven.h - C-ABI of the GB300-native Eleven Renderer sample path.
+ *
+ * One shared library (libeleven.so) exports everything below with C linkage,
+ * plain pointers and sizes.  It replaces the reference's render boundary
+ * (src/tfg-pathtracer/kernel.h:78-84, defined in kernel.cu:566-724):
+ *
+ *   reference                                   replaced by
+ *   cudaError_t renderSetup(Scene*)             er_scene_create / er_scene_load
+ *     (kernel.h:81, kernel.cu:566-661)            (scene upload + BVH build)
+ *   cudaError_t renderCuda(Scene*, int spp)     er_render
+ *     (kernel.h:79, kernel.cu:665-686)
+ *   cudaError_t getBuffers(RenderData&, int*,   er_render output buffers /
+ *     int) (kernel.h:83, kernel.cu:688-710)       er_film_read
+ *   int getSamples() (kernel.h:85,              er_film_read (samples array)
+ *     kernel.cu:712-724)
+ *   BVH::transverse (BVH.hpp:120-157) via      er_trace_closest (parity gate)
+ *     throwRay (kernel.cu:152-173)
+ *
+ * Every call returns an er_status; no C++ exception crosses the ABI and no
+ * device-side trap is used: device checks set an error word that the host
+ * turns into ER_ERR_DEVICE_CHECK / ER_ERR_TIMEOUT.
+ *
+ * Threading: calls on one handle are serialised by the caller; handles are
+ * independent of each other (no process globals).  All work of a handle is
+ * issued on the stream given at creation (NULL = a stream owned by the handle).
+ */
+#ifndef ELEVEN_H
+#define ELEVEN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ER_ABI_VERSION 1
+
+typedef int32_t er_status;
+enum {
+  ER_OK = 0,
+  ER_ERR_INVALID_ARG = 1,   /* NULL pointer, negative size, NaN parameter ... */
+  ER_ERR_IO = 2,            /* missing / unreadable scene file */
+  ER_ERR_PARSE = 3,         /* malformed JSON / OBJ / MTL / BMP / HDR */
+  ER_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+  ER_ERR_OOM = 5,           /* device or host allocation failed / over cap */
+  ER_ERR_DEVICE_CHECK = 6,  /* a kernel's own bounds check fired */
+  ER_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
+  ER_ERR_UNSUPPORTED = 8,   /* feature not available on this device / build */
+  ER_ERR_NO_DEVICE = 9      /* no CUDA device visible */
+};
+
+/* Static description of a status code. */
+const char* er_status_string(er_status s);
+/* Detail message of the last failing call on this thread ("" if none). */
+const char* er_last_error(void);
+/* ABI version of the loaded library (ER_ABI_VERSION). */
+int32_t er_abi_version(void);
+
+/* ---------------------------------------------------------------- scene -- */
+
+/* Camera.hpp:6-40.  rotation is XYZ Euler in degrees (kernel.cu:297-306);
+ * aperture is the reference's f-number: lens diameter = focal/aperture
+ * (kernel.cu:316). */
+typedef struct er_camera {
+  int32_t x_res, y_res;
+  float focal_length;
+  float sensor_width;
+  float sensor_height;
+  float aperture;
+  float focus_distance;
+  float position[3];
+  float rotation[3];
+  int32_t bokeh;
+} er_camera;
+
+/* Material.hpp:8-37.  Texture ids index er_scene_desc.textures, -1 = none. */
+typedef struct er_material {
+  int32_t albedo_tex, emission_tex, roughness_tex, metallic_tex, normal_tex;
+  float albedo[3];
+  float emission[3];
+  float roughness, metallic, clearcoat_gloss, clearcoat, anisotropic, eta,
+      transmission, specular, specular_tint, sheen_tint, subsurface, sheen;
+} er_material;
+
+/* Texture.hpp:196-214: float RGB texels, row-major, row 0 first as stored
+ * after loading (loaders flip BMPs on load, Texture.hpp:230). */
+typedef struct er_texture {
+  int32_t width, height;
+  const float* data; /* width*height*3 */
+  float x_tile, y_tile, x_offset, y_offset;
+} er_texture;
+
+/* PointLight.hpp:6-18 */
+typedef struct er_point_light {
+  float position[3];
+  float radiance[3];
+} er_point_light;
+
+/* Flat triangle soup in the reference's Tri layout (Tri.hpp:13-19), one
+ * entry per triangle, vertices in winding order. */
+typedef struct er_scene_desc {
+  er_camera camera;
+  int64_t tri_count;
+  const float* positions;    /* tri_count*9                                 */
+  const float* normals;      /* tri_count*9, NULL = zero normals            */
+  const float* uvs;          /* tri_count*6 (u,v per vertex), NULL = zeros  */
+  const float* tangents;     /* tri_count*9, NULL = zero tangents           */
+  const float* tangent_sign; /* tri_count, NULL = +1                         */
+  const int32_t* tri_object; /* tri_count: mesh object of each triangle     */
+  int32_t object_count;
+  const int32_t* object_material; /* object_count: material of each object */
+  int32_t material_count;
+  const er_material* materials;
+  int32_t texture_count;
+  const er_texture* textures;
+  int32_t light_count;
+  const er_point_light* lights;
+  er_texture env; /* environment map (HDRI.hpp); constant colours are given as
+                     a filled texture, as HDRI(Vector3) does (HDRI.hpp:22-38) */
+  /* Optional per-triangle tie key: among hits at exactly equal reference
+   * distance the lowest key wins.  NULL = triangle index. */
+  const uint32_t* tie_key;
+} er_scene_desc;
+
+/* BVH node formats. */
+enum { ER_BVH_FP32 = 0, ER_BVH_Q8 = 1 };
+
+typedef struct er_scene_opts {
+  int32_t bvh_format;     /* ER_BVH_FP32 or ER_BVH_Q8 */
+  int32_t max_leaf_tris;  /* 1..8, 0 = default (4) */
+  int32_t device;         /* CUDA device ordinal */
+  void* stream;           /* cudaStream_t, NULL = handle-owned stream */
+} er_scene_opts;
+
+typedef struct er_scene er_scene;
+
+typedef struct er_scene_info {
+  int64_t tri_count;
+  int64_t node_count;
+  int64_t leaf_count;
+  int64_t device_bytes;     /* bytes held on the device by the handle */
+  double bvh_build_ms;      /* host BVH build time */
+  double upload_ms;         /* host->device upload time */
+  float scene_lo[3], scene_hi[3];
+  float max_shading_offset; /* bound on |shading position - geometric hit| */
+  int32_t bvh_depth;
+  int32_t bvh_format;
+} er_scene_info;
+
+/* Build a scene from arrays (the harness / generator path). */
+er_status er_scene_create(const er_scene_desc* desc, const er_scene_opts* opts,
+                          er_scene** out);
+/* Load a reference scene folder: scene.json, scene.obj, scene.mtl, HDRI/ and
+ * the textures the .mtl names (SceneLoader.hpp:7-143).  x_res/y_res come
+ * from scene.json. */
+er_status er_scene_load(const char* dir, const er_scene_opts* opts,
+                        er_scene** out);
+er_status er_scene_info_get(const er_scene* scene, er_scene_info* out);
+/* Replace the camera of a built scene (no BVH rebuild). */
+er_status er_scene_set_camera(er_scene* scene, const er_camera* cam);
+er_status er_scene_free(er_scene* scene);
+
+/* ---------------------------------------------------------------- render -- */
+
+enum {
+  ER_RENDER_DEVICE_OUT = 1u << 0, /* output pointers are device pointers    */
+  ER_RENDER_ACCUM_FP64 = 1u << 1, /* FP64 per-pixel sums instead of the
+                                     reference FP32 running mean            */
+  ER_RENDER_AOV = 1u << 2,        /* also write NORMAL/TANGENT/BITANGENT     */
+  ER_RENDER_ENV_ALIAS = 1u << 3,  /* env sampling through the FP64-built
+                                     alias table of the reference's effective
+                                     texel distribution                     */
+  ER_RENDER_CONTINUE = 1u << 4,   /* add samples to the film of the previous
+                                     call instead of clearing it            */
+  ER_RENDER_NO_OUTPUT = 1u << 5   /* render into the film only              */
+};
+
+typedef struct er_render_opts {
+  int32_t spp;            /* samples per pixel of this call                 */
+  int32_t sample_begin;   /* first sample index (for split / resumed runs) */
+  int32_t max_depth;      /* MAXBOUNCES (Definitions.h:9); 0 = 5            */
+  int32_t spp_per_wave;   /* samples per pixel traced together; 0 = auto    */
+  uint64_t seed;          /* RNG key                                        */
+  uint32_t flags;         /* ER_RENDER_*                                    */
+  int32_t reserved;
+} er_render_opts;
+
+typedef struct er_render_stats {
+  double ms;              /* device time of the call (CUDA events)          */
+  int64_t samples;        /* path samples traced                            */
+  int64_t rays_closest;   /* extension rays traced                          */
+  int64_t rays_shadow;    /* shadow rays traced                             */
+  int64_t path_vertices;  /* Σ bounce counts = reference "paths" counter    */
+  int64_t kernel_launches;
+} er_render_stats;
+
+/* Render `opts->spp` samples per pixel.  beauty (and, with ER_RENDER_AOV,
+ * normal/tangent/bitangent) are W*H*4 floats in the reference's pass layout
+ * (RGBA, alpha = 1, row y = 0 at the top of the image as the reference's
+ * vertically flipped index, kernel.cu:378).  samples and pathcount are W*H
+ * uint32 (dev_samples / dev_pathcount, kernel.cu:44-45).  Any output pointer
+ * may be NULL.  stats may be NULL. */
+er_status er_render(er_scene* scene, const er_render_opts* opts, float* beauty,
+                    float* normal, float* tangent, float* bitangent,
+                    uint32_t* samples, uint32_t* pathcount,
+                    er_render_stats* stats);
+
+/* Read the current film (after one or more er_render calls). */
+er_status er_film_read(er_scene* scene, uint32_t flags, float* beauty,
+                       float* normal, float* tangent, float* bitangent,
+                       uint32_t* samples, uint32_t* pathcount);
+
+/* Per-path debug output of one wave: radiance (before the clamp of
+ * kernel.cu:447) and bounce count of path (pixel p, sample s) for
+ * s in [sample_begin, sample_begin+spp).  radiance is spp*W*H*3 floats,
+ * bounces spp*W*H int32, both indexed [s][p] with p the output pixel index. */
+er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
+                          float* radiance, int32_t* bounces);
+
+/* ----------------------------------------------------------------- trace -- */
+
+enum {
+  ER_TRACE_DEVICE_PTRS = 1u << 0, /* all pointers are device pointers        */
+  ER_TRACE_NORMALIZED = 1u << 1,  /* directions already went through the
+                                     reference Ray constructor normalisation  */
+  ER_TRACE_STATS = 1u << 2        /* count node / triangle tests             */
+};
+
+typedef struct er_trace_stats {
+  double ms;
+  int64_t node_visits;
+  int64_t box_tests;
+  int64_t tri_tests;
+} er_trace_stats;
+
+/* Closest hit of n rays, each 6 floats (origin xyz, direction xyz).  The
+ * direction is normalised as Ray.hpp:14-18 does unless ER_TRACE_NORMALIZED.
+ * tri_id[i] = index of the hit triangle in the scene desc or -1; dist[i] =
+ * |hit position - origin| with the reference's hit position (smooth-shading
+ * position when convex, Tri.hpp:74-92); uv[2i..2i+1] = barycentric (u, v).
+ * dist / uv may be NULL. */
+er_status er_trace_closest(er_scene* scene, const float* rays, int64_t n,
+                           int32_t* tri_id, float* dist, float* uv,
+                           uint32_t flags, er_trace_stats* stats);
+
+/* ----------------------------------------------------------------- image -- */
+
+/* Reference output step (main.cpp:150-165, PostProcessing.cpp:30-33):
+ * clamp to [0,1], approximate pow(x, 1/2.2) by the fastPow bit trick
+ * (stb_image.h:127-135), *255, truncate.  rgba_in is W*H*4 floats on the
+ * host, out is W*H*4 bytes. */
+er_status er_encode_ldr(const float* rgba_in, int32_t width, int32_t height,
+                        uint8_t* out);
+/* Write W*H*4 bytes as PNG (what the reference writes, also for .bmp names)
+ * or, when as_bmp != 0, as a 24-bit BMP. */
+er_status er_write_image(const char* path, const uint8_t* rgba, int32_t width,
+                         int32_t height, int32_t as_bmp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ELEVEN_H */
