@@ -284,6 +284,7 @@ void orc_encode_ldr(const float* rgba, int64_t n, uint8_t* out) {
   for (int64_t i = 0; i < n; i++) {
     float v = clampf_(rgba[i], 0.0f, 1.0f);
     double e = orc_fastpow((double)v, 1.0 / 2.2) * 255.0;
+    if (!(e >= 0.0 && e < 256.0)) e = 0.0; /* NaN input: defined as 0 */
     out[i] = (uint8_t)(int32_t)e;
   }
 }

@@ -9,11 +9,15 @@
  */
 #include "orc.h"
 
-/* Texture.hpp:95-112: tile/offset, truncation, C remainder (negative
- * indices are not wrapped). */
+/* Texture.hpp:95-112: tile/offset, truncation, C remainder.  A negative
+ * remainder (u < 0, negative offsets) makes the reference read outside the
+ * texel array; it is wrapped into range here instead (defined behaviour,
+ * identical to the reference for every in-range index). */
 v3 orc_tex_coord(const orc_tex* t, int32_t x, int32_t y) {
   x = f2i_dev(t->xTile * ((float)x + t->xOffset * (float)t->w)) % t->w;
   y = f2i_dev(t->yTile * ((float)y + t->yOffset * (float)t->h)) % t->h;
+  if (x < 0) x += t->w;
+  if (y < 0) y += t->h;
   int64_t i = 3 * ((int64_t)y * t->w + x);
   return V3(t->data[i], t->data[i + 1], t->data[i + 2]);
 }
@@ -74,10 +78,12 @@ void orc_hdri_cdf(const orc_tex* t, float* cdf, float* radianceSum) {
   *radianceSum = sum;
 }
 
-/* HDRI.hpp:130-142: returns `to`, not an exact lower bound. */
+/* HDRI.hpp:130-142: returns `to`, not an exact lower bound.  Bounded to 64
+ * steps: with a NaN CDF (all-black environment, zero sum) the reference's
+ * loop never ends. */
 int32_t orc_hdri_search(const float* arr, float value, int32_t length) {
   int32_t from = 0, to = length - 1;
-  while (to - from > 0) {
+  for (int it = 0; it < 64 && to - from > 0; it++) {
     int32_t m = from + (to - from) / 2;
     if (value == arr[m]) return m;
     if (value < arr[m]) to = m - 1;

@@ -1,0 +1,124 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the oracle.
+
+Hit IDs are compared bit for bit with the reference's traversal restated in
+the oracle; images are compared per path (same random numbers) and per
+pixel (relative RMSE).
+"""
+import numpy as np
+import pytest
+
+import _oracle as O
+from eleven import _abi as A
+from eleven import _lib, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+@pytest.fixture(scope="module")
+def c0():
+    arrays = scenes.config0(x_res=96, y_res=72)
+    return arrays, _lib.Scene(arrays), O.OrcScene(arrays)
+
+
+def classify(orc, rays, gpu_tri, gpu_dist, ref_tri, ref_dist):
+    """Mismatching rays: tie (same reference distance) or not."""
+    bad = np.nonzero(gpu_tri != ref_tri)[0]
+    ties = [i for i in bad if gpu_dist[i] == ref_dist[i]]
+    return bad, ties
+
+
+def test_closest_ids_random_rays(c0):
+    arrays, scene, orc = c0
+    rays = scenes.random_rays(arrays, 200_000, seed=3)
+    tri, dist, _, _ = scene.trace(rays)
+    rtri, rdist = orc.trace(rays)
+    bad, ties = classify(orc, rays, tri, dist, rtri, rdist)
+    assert len(bad) == len(ties), f"{len(bad) - len(ties)} non-tie hit-id mismatches of {len(rays)}"
+    ok = tri == rtri
+    assert np.array_equal(dist[ok].view(np.uint32), rdist[ok].view(np.uint32))
+    assert (tri >= 0).sum() > 10_000
+
+
+def test_closest_ids_camera_rays(c0):
+    """Primary rays generated on the GPU, traced on both sides."""
+    arrays, scene, orc = c0
+    rays = scenes.random_rays(arrays, 1, seed=1)  # placeholder for shape
+    W, H = scene.resolution
+    rng = np.random.default_rng(7)
+    cam = arrays.camera
+    # pinhole rays through pixel centres, as the reference camera builds them
+    xs, ys = np.meshgrid(np.arange(W), np.arange(H))
+    sw = np.float32(scenes.SENSOR_WIDTH)
+    sh = np.float32(sw * (np.float32(H) / np.float32(W)))
+    px = (xs / W * sw - sw / 2 + rng.uniform(-0.5, 0.5, xs.shape) * sw / W).astype(np.float32)
+    py = (ys / H * sh - sh / 2 + rng.uniform(-0.5, 0.5, ys.shape) * sh / H).astype(np.float32)
+    o = np.broadcast_to(np.asarray(cam["position"], np.float32), (H * W, 3))
+    d = np.stack([px.ravel(), py.ravel(), np.full(H * W, cam["focal_length"], np.float32)], 1)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    tri, dist, _, _ = scene.trace(rays)
+    rtri, rdist = orc.trace(rays)
+    bad, ties = classify(orc, rays, tri, dist, rtri, rdist)
+    assert len(bad) == len(ties)
+
+
+def test_q8_bvh_same_hits(c0):
+    arrays, scene, orc = c0
+    q8 = _lib.Scene(arrays, bvh_format=A.ER_BVH_Q8)
+    rays = scenes.random_rays(arrays, 200_000, seed=5)
+    t1, d1, _, _ = scene.trace(rays)
+    t2, d2, _, _ = q8.trace(rays)
+    assert np.array_equal(t1, t2)
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+    q8.close()
+
+
+def test_render_paths_match_oracle(c0):
+    arrays, scene, orc = c0
+    rad, b = scene.render_paths(spp=2, max_depth=4, seed=11)
+    rrad, rb = orc.render_paths(spp=2, max_depth=4, seed=11)
+    same_b = (b == rb).mean()
+    close = np.isclose(rad, rrad, rtol=1e-3, atol=1e-5).all(axis=2)
+    both_nan = np.isnan(rad).any(2) & np.isnan(rrad).any(2)
+    frac = (close | both_nan).mean()
+    assert same_b > 0.99, f"bounce counts agree on {same_b:.4f} of paths"
+    assert frac > 0.98, f"per-path radiance agrees on {frac:.4f} of paths"
+
+
+def test_render_image_matches_oracle(c0):
+    arrays, scene, orc = c0
+    out = scene.render(spp=8, max_depth=4, seed=3)
+    ref = orc.render(spp=8, max_depth=4, seed=3)
+    e = rel_rmse(out["beauty"][:, :3], ref["beauty"][:, :3])
+    assert e < 0.03, e
+    assert (out["beauty"][:, 3] == 1).all()
+    # samples / pathcount counters (kernel.cu:445,477)
+    assert np.abs(out["samples"].astype(np.int64) - ref["samples"]).max() <= 1
+    assert np.abs(out["pathcount"].astype(np.int64) - ref["pathcount"].astype(np.int64)).mean() < 0.5
+
+
+def test_fp64_accumulation_close_to_fp32(c0):
+    arrays, scene, orc = c0
+    a = scene.render(spp=8, max_depth=4, seed=3)["beauty"]
+    b = scene.render(spp=8, max_depth=4, seed=3, flags=A.ER_RENDER_ACCUM_FP64)["beauty"]
+    assert rel_rmse(b[:, :3], a[:, :3]) < 1e-5
+
+
+def test_continue_equals_single_call(c0):
+    arrays, scene, orc = c0
+    one = scene.render(spp=4, max_depth=3, seed=9)["beauty"]
+    scene.render(spp=2, max_depth=3, seed=9)
+    two = scene.render(spp=2, max_depth=3, seed=9, sample_begin=2, flags=A.ER_RENDER_CONTINUE)["beauty"]
+    assert np.array_equal(one, two)
+
+
+def test_wave_split_is_deterministic(c0):
+    arrays, scene, orc = c0
+    a = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=4)["beauty"]
+    b = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=1)["beauty"]
+    assert np.array_equal(a, b)

@@ -1,0 +1,168 @@
+// Host-side internals of libeleven: device scene layout, film, status helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "eleven.h"
+
+namespace er {
+
+// ---------------------------------------------------------------- status --
+
+void set_error(const std::string& msg);
+er_status fail(er_status s, const std::string& msg);
+er_status cuda_fail(cudaError_t e, const char* what);
+
+#define ER_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return ::er::cuda_fail(e_, #call); \
+  } while (0)
+
+// ------------------------------------------------------------ BVH layout --
+//
+// FP32 BVH4 node, 128 bytes (two 64-byte lines), loaded as 8 float4:
+//   [0] lo.x[4] [1] hi.x[4] [2] lo.y[4] [3] hi.y[4] [4] lo.z[4] [5] hi.z[4]
+//   [6] child[4] (int bits)  [7] shading-offset bound of each child (float)
+// child: >= 0 internal node index; kEmpty = no child; otherwise a leaf:
+//   bit 31 set, bits 30..27 = tri count - 1, bits 26..0 = first leaf slot.
+constexpr int32_t kEmpty = -1;
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kLeafCountShift = 27;
+constexpr uint32_t kLeafFirstMask = (1u << 27) - 1;
+constexpr int kMaxLeafTris = 16;
+constexpr int64_t kMaxTris = (int64_t)kLeafFirstMask - 1;
+
+inline int32_t make_leaf(uint32_t first, uint32_t count) {
+  return (int32_t)(kLeafBit | ((count - 1u) << kLeafCountShift) | first);
+}
+
+// 8-bit quantised BVH4 node, 64 bytes:
+//   [0] origin.xyz (float), w = exponent bytes e.x | e.y<<8 | e.z<<16
+//   [1] qlo.x[4] qhi.x[4] qlo.y[4] qhi.y[4] as bytes
+//   [2] qlo.z[4] qhi.z[4], child[0..1]
+//   [3] child[2..3], shading-offset bound (max of the 4 children), pad
+// child box = origin + q * 2^e, rounded outward at build time.
+struct QNode {
+  float ox, oy, oz;
+  uint32_t ex;
+  uint8_t qlx[4], qhx[4], qly[4], qhy[4];
+  uint8_t qlz[4], qhz[4];
+  int32_t child01[2];
+  int32_t child23[2];
+  float delta;
+  uint32_t pad;
+};
+static_assert(sizeof(QNode) == 64, "QNode is one 64-byte line");
+
+struct BuildResult {
+  std::vector<float> nodes;        // 32 floats per FP32 node
+  std::vector<QNode> qnodes;       // quantised form (same topology)
+  std::vector<int32_t> order;      // leaf slot -> desc triangle index
+  int64_t node_count = 0, leaf_count = 0;
+  int32_t depth = 0;
+  float max_delta = 0;
+};
+
+// Builds the SAH BVH4 over the desc's triangles (bvh_build.cpp).
+er_status build_bvh4(const er_scene_desc* d, int max_leaf, BuildResult* out);
+void quantize_bvh4(BuildResult* r);
+// Bound on |shading position - geometric hit| for triangle i (Tri.hpp:74-92).
+double shading_offset_bound(const er_scene_desc* d, int64_t i);
+
+// ----------------------------------------------------------- device scene --
+
+// Texture descriptor on the device (Texture.hpp:196-214).
+struct DevTex {
+  int32_t w, h;
+  int64_t offset;  // float4 texel offset into the texel pool
+  float x_tile, y_tile, x_offset, y_offset;
+};
+
+// Camera with the per-ray trigonometry hoisted (kernel.cu:297-306).
+struct DevCamera {
+  int32_t x_res, y_res;
+  float focal_length, sensor_width, sensor_height, aperture, focus_distance;
+  float px, py, pz;
+  float cx, sx, cy, sy, cz, sz;  // cosf / sinf of the rotation in radians
+  int32_t bokeh;
+};
+
+// Material as the shader reads it (Material.hpp:8-37).
+struct DevMaterial {
+  int32_t albedo_tex, emission_tex, roughness_tex, metallic_tex, normal_tex, pad0, pad1, pad2;
+  float albedo[4];
+  float emission[4];
+  float roughness, metallic, clearcoat_gloss, clearcoat, anisotropic, eta, transmission, specular;
+  float specular_tint, sheen_tint, subsurface, sheen;
+};
+
+struct DevScene {
+  const float4* nodes;   // FP32 BVH4 (8 float4 per node)
+  const uint4* qnodes;   // quantised BVH4 (4 uint4 per node) or null
+  const float4* tri_v;   // 3 float4 per leaf slot: v0|desc id, v1|tie key, v2|material
+  const float4* tri_n;   // 3 float4 per leaf slot: n0|tangent sign, n1, n2
+  const float2* tri_uv;  // 3 float2 per leaf slot
+  const float4* tri_t;   // 3 float4 per leaf slot (tangents) or null
+  const DevMaterial* mats;
+  const DevTex* texs;
+  const float4* texels;  // RGB(A) texel pool
+  const er_point_light* lights;
+  DevTex env;
+  const float* cdf;      // env CDF, w*h+1 floats (HDRI.hpp:107-128)
+  const int32_t* alias_idx;   // env alias table (w*h) or null
+  const float* alias_prob;
+  float radiance_sum;
+  int32_t n_lights;
+  int32_t n_mats;
+  int32_t n_texs;
+  int64_t n_tris;
+  int64_t n_nodes;
+  float scene_eps;       // absolute slack for conservative box tests
+  int32_t use_q8;
+  DevCamera cam;
+};
+
+struct Film {
+  int32_t w = 0, h = 0;
+  float4* beauty = nullptr;
+  float4* aov[3] = {nullptr, nullptr, nullptr};
+  double* sum = nullptr;       // FP64 sums (3 per pixel) in FP64 mode
+  uint32_t* samples = nullptr;
+  uint32_t* pathcount = nullptr;
+  bool aov_on = false;
+};
+
+struct Wave;  // wavefront buffers (render.cu)
+
+}  // namespace er
+
+struct er_scene {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  er::DevScene dev{};
+  std::vector<void*> allocs;   // device allocations owned by the handle
+  int64_t device_bytes = 0;
+  er_scene_info info{};
+  er_camera camera{};
+  int num_sms = 0;
+  er::Film film;
+  er::Wave* wave = nullptr;
+  uint32_t* err_word = nullptr;   // device error word (bounds / timeout)
+  unsigned long long* d_stats = nullptr;  // device ray counters
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace er {
+er_status dev_alloc(er_scene* s, void** p, size_t bytes);
+er_status upload(er_scene* s, void** p, const void* host, size_t bytes);
+DevCamera make_dev_camera(const er_camera& c);
+void free_wave(er_scene* s);
+void free_film(er_scene* s);
+er_status check_device_error(er_scene* s);
+}  // namespace er

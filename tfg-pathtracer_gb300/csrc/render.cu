@@ -1,0 +1,676 @@
+// Wavefront path tracer: the sample loop of the reference's renderingKernel
+// (kernel.cu:369-481) split into stages that run over compacted queues:
+//
+//   raygen -> [ extend (closest hit) -> shade -> shadow ] x max_depth -> accumulate
+//
+// One wave traces spp_wave samples of every pixel.  Paths are indexed
+// p = s * npix + pix; per-path state lives in SoA arrays, queues hold
+// (origin|path, direction) pairs and are appended with warp ballots + one
+// atomic per warp.  Radiance contributions of a vertex are resolved in the
+// reference's order (kernel.cu:351-357) once its two shadow rays are done,
+// and samples are accumulated per pixel in sample order, so the image does
+// not depend on queue order.
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace er {
+
+// Device view of the wave buffers (passed to kernels by value).
+struct WaveView {
+  bool aov = false;
+  float4* thr = nullptr;
+  float4* light = nullptr;
+  float4* pend = nullptr;  // 4 per path
+  uint8_t* vis = nullptr;  // 2 per path
+  int32_t* bounces = nullptr;
+  float4* aovs = nullptr;  // 3 per path
+  float4* q_o[2] = {nullptr, nullptr};
+  float4* q_d[2] = {nullptr, nullptr};
+  float4* hits = nullptr;
+  float4* s_o = nullptr;
+  float4* s_d = nullptr;
+  float4* s_p = nullptr;
+  int32_t* counts = nullptr;       // [0],[1] extension queues, [2] shadow queue
+  unsigned long long* stats = nullptr;  // [0] closest rays [1] shadow rays (owned by the scene)
+};
+
+struct Wave {
+  int64_t cap = 0;
+  WaveView v;
+  std::vector<void*> mem;
+};
+
+struct WaveParams {
+  int32_t W, H, npix, spp_wave, sample_base, max_depth;
+  uint32_t k0, k1;
+  uint32_t flags;
+};
+
+namespace {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append: one atomic per warp, slots ordered by lane.
+__device__ __forceinline__ int32_t warp_append(int32_t* counter, bool pred) {
+  unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
+  int32_t base = 0;
+  if (mask) {
+    int leader = __ffs(mask) - 1;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  }
+  unsigned lt = (1u << lane_id()) - 1u;
+  return base + __popc(mask & lt);
+}
+
+// kernel.cu:378: output index of thread pixel (x, y)
+__device__ __forceinline__ int32_t out_index(const WaveParams& P, int32_t x, int32_t y) {
+  return P.W * (P.H - y - 1) + x;
+}
+
+__global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n) {
+  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) {
+    w.counts[0] = n;
+    w.counts[1] = 0;
+    w.counts[2] = 0;
+  }
+  if (p >= n) return;
+  int32_t pix = p % P.npix, s = p / P.npix;
+  int32_t x = pix % P.W, y = pix / P.W;
+  uint32_t idx = (uint32_t)out_index(P, x, y);
+  uint32_t sample = (uint32_t)(P.sample_base + s);
+  uint4 a = philox(make_uint4(idx, sample, 0u, 0u), P.k0, P.k1);
+  uint4 b = philox(make_uint4(idx, sample, 1u, 0u), P.k0, P.k1);
+  f3 o, d;
+  camera_ray(S.cam, x, y, u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), o, d);
+  w.q_o[0][p] = make_float4(o.x, o.y, o.z, __int_as_float(p));
+  w.q_d[0][p] = make_float4(d.x, d.y, d.z, 0.0f);
+  w.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+  w.light[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+  w.pend[4 * (size_t)p + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  w.bounces[p] = P.max_depth;
+  if (w.aov) {
+    w.aovs[3 * (size_t)p] = make_float4(0, 0, 0, 0);
+    w.aovs[3 * (size_t)p + 1] = make_float4(0, 0, 0, 0);
+    w.aovs[3 * (size_t)p + 2] = make_float4(0, 0, 0, 0);
+  }
+}
+
+template <bool Q8>
+__global__ void __launch_bounds__(kTravBlock) k_extend(DevScene S, WaveView w, int32_t qin, uint32_t* err) {
+  __shared__ int2 stk[kSmemStack * kTravBlock];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counts[qin ^ 1] = 0;
+    w.counts[2] = 0;
+    atomicAdd(&w.stats[0], (unsigned long long)w.counts[qin]);
+  }
+  const int32_t n = w.counts[qin];
+  const float4* qo = w.q_o[qin];
+  const float4* qd = w.q_d[qin];
+  TravStats st{0, 0, 0};
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 a = qo[i], b = qd[i];
+    TravResult r = traverse<kClosest, Q8, false>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk1(0.f), 0.f,
+                                                 stk + threadIdx.x, st, err);
+    w.hits[i] = make_float4(r.t, r.u, r.v, __int_as_float(r.slot));
+  }
+}
+
+template <bool Q8>
+__global__ void __launch_bounds__(kTravBlock) k_shadow(DevScene S, WaveView w, uint32_t* err) {
+  __shared__ int2 stk[kSmemStack * kTravBlock];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[1], (unsigned long long)w.counts[2]);
+  const int32_t n = w.counts[2];
+  TravStats st{0, 0, 0};
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 a = w.s_o[i], b = w.s_d[i];
+    int32_t tag = __float_as_int(a.w);
+    f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
+    bool occ;
+    if (tag & 1) {
+      float4 q = w.s_p[i];
+      occ = traverse<kPoint, Q8, false>(S, o, d, mk(q.x, q.y, q.z), b.w, stk + threadIdx.x, st, err).occluded;
+    } else {
+      occ = traverse<kAny, Q8, false>(S, o, d, mk1(0.f), 0.f, stk + threadIdx.x, st, err).occluded;
+    }
+    w.vis[tag] = occ ? 0 : 1;  // tag = 2*path + type
+  }
+}
+
+// Resolve the pending MIS terms of a path's last shaded vertex
+// (kernel.cu:351-355,433): light += reduction * ((w1*H + w2*P) + w3*B),
+// with an occluded strategy contributing w*0 (NaN when its weight is).
+__device__ __forceinline__ void resolve(const WaveView& w, int32_t p, float4& L) {
+  float4 tB = w.pend[4 * (size_t)p + 2];
+  uint32_t fl = __float_as_uint(tB.w);
+  if (!(fl & 1u)) return;
+  float4 tH = w.pend[4 * (size_t)p];
+  float4 tP = w.pend[4 * (size_t)p + 1];
+  float4 rp = w.pend[4 * (size_t)p + 3];
+  bool vH = w.vis[2 * (size_t)p] != 0;
+  bool vP = (fl & 2u) ? (w.vis[2 * (size_t)p + 1] != 0) : true;
+  float hx = vH ? tH.x : tH.w, hy = vH ? tH.y : tH.w, hz = vH ? tH.z : tH.w;
+  float px = vP ? tP.x : tP.w, py = vP ? tP.y : tP.w, pz = vP ? tP.z : tP.w;
+  L.x = __fadd_rn(L.x, __fmul_rn(__fadd_rn(__fadd_rn(hx, px), tB.x), rp.x));
+  L.y = __fadd_rn(L.y, __fmul_rn(__fadd_rn(__fadd_rn(hy, py), tB.y), rp.y));
+  L.z = __fadd_rn(L.z, __fmul_rn(__fadd_rn(__fadd_rn(hz, pz), tB.z), rp.z));
+  w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
+}
+
+__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParams P, int32_t qin, int32_t bounce) {
+  const int32_t n = w.counts[qin];
+  const float4* qo = w.q_o[qin];
+  const float4* qd = w.q_d[qin];
+  const int32_t qout = qin ^ 1;
+  const bool last = bounce + 1 >= P.max_depth;
+  for (int32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    int32_t i = base + threadIdx.x;
+    bool valid = i < n;
+    bool push_next = false, push_env = false, push_pt = false;
+    f3 next_o = mk1(0), next_d = mk1(0), env_o = mk1(0), env_d = mk1(0), pt_o = mk1(0), pt_d = mk1(0),
+       pt_p = mk1(0);
+    float pt_dist = 0.f;
+    int32_t p = 0;
+    if (valid) {
+      float4 a = qo[i], b = qd[i];
+      p = __float_as_int(a.w);
+      f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
+      float4 L = w.light[p];
+      resolve(w, p, L);
+      float4 T4 = w.thr[p];
+      f3 thr = mk(T4.x, T4.y, T4.z);
+      float4 h = w.hits[i];
+      int32_t slot = __float_as_int(h.w);
+      if (slot < 0) {
+        // kernel.cu:414-419: environment on escape, no MIS weight
+        float eu, ev;
+        spherical_mapping(-d, eu, ev);
+        f3 e = tex_uv(S, S.env, eu, ev);
+        L.x = __fadd_rn(L.x, __fmul_rn(e.x, thr.x));
+        L.y = __fadd_rn(L.y, __fmul_rn(e.y, thr.y));
+        L.z = __fadd_rn(L.z, __fmul_rn(e.z, thr.z));
+        w.bounces[p] = bounce;
+      } else {
+        // Tri.hpp:70-92 + 153-157 rebuilt from (t, u, v) with the same ops
+        const float4* tv = S.tri_v + 3 * (size_t)slot;
+        const float4* tn = S.tri_n + 3 * (size_t)slot;
+        float4 v0 = __ldg(tv), v1 = __ldg(tv + 1), v2 = __ldg(tv + 2);
+        float4 n0 = __ldg(tn), n1 = __ldg(tn + 1), n2 = __ldg(tn + 2);
+        float t = h.x, u = h.y, v = h.z;
+        f3 sn;
+        f3 pos = ref_position(o, d, t, u, v, from4(v0), from4(v1), from4(v2), from4(n0), from4(n1), from4(n2), &sn);
+        const float2* tuv = S.tri_uv + 3 * (size_t)slot;
+        float2 uv0 = __ldg(tuv), uv1 = __ldg(tuv + 1), uv2 = __ldg(tuv + 2);
+        float tu = __fadd_rn(__fadd_rn(uv0.x, __fmul_rn(__fsub_rn(uv1.x, uv0.x), u)), __fmul_rn(__fsub_rn(uv2.x, uv0.x), v));
+        float tvv = __fadd_rn(__fadd_rn(uv0.y, __fmul_rn(__fsub_rn(uv1.y, uv0.y), u)), __fmul_rn(__fsub_rn(uv2.y, uv0.y), v));
+        f3 tg = mk1(0.f), bt = mk1(0.f);
+        if (S.tri_t) {
+          const float4* tt = S.tri_t + 3 * (size_t)slot;
+          f3 g0 = from4(__ldg(tt)), g1 = from4(__ldg(tt + 1)), g2 = from4(__ldg(tt + 2));
+          tg = xadd(xadd(g0, xscale(xsub(g1, g0), u)), xscale(xsub(g2, g0), v));
+          bt = xscale(xcross(sn, tg), n0.w);
+        }
+        // kernel.cu:54-119 generateHitData
+        const DevMaterial& M = S.mats[__float_as_int(v2.w)];
+        HitData hd;
+        hd.albedo = M.albedo_tex < 0 ? mk(M.albedo[0], M.albedo[1], M.albedo[2]) : tex_uv(S, S.texs[M.albedo_tex], tu, tvv);
+        hd.emission = M.emission_tex < 0 ? mk(M.emission[0], M.emission[1], M.emission[2])
+                                         : tex_uv(S, S.texs[M.emission_tex], tu, tvv);
+        float rough = M.roughness_tex < 0 ? M.roughness : tex_uv(S, S.texs[M.roughness_tex], tu, tvv).x;
+        float metal = M.metallic_tex < 0 ? M.metallic : tex_uv(S, S.texs[M.metallic_tex], tu, tvv).x;
+        if (M.normal_tex < 0) {
+          hd.normal = sn;
+        } else {
+          f3 c = tex_uv(S, S.texs[M.normal_tex], tu, tvv);
+          f3 ln = c * 2.0f - mk1(1.0f);
+          hd.normal = normalized(tg * ln.x - bt * ln.y + sn * ln.z);
+        }
+        hd.roughness = powf(rough, 2.2f);
+        hd.metallic = powf(metal, 2.2f);
+        hd.clearcoatGloss = M.clearcoat_gloss;
+        hd.clearcoat = M.clearcoat;
+        hd.anisotropic = M.anisotropic;
+        hd.transmission = M.transmission;
+        hd.specular = M.specular;
+        hd.specularTint = M.specular_tint;
+        hd.sheenTint = M.sheen_tint;
+        hd.subsurface = M.subsurface;
+        hd.sheen = M.sheen;
+
+        int32_t pix = p % P.npix, s = p / P.npix;
+        uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
+        uint4 rn = philox(make_uint4(idx, (uint32_t)(P.sample_base + s), 2u + (uint32_t)bounce, 0u), P.k0, P.k1);
+        DisneyCtx C = disney_ctx(hd, d);
+        f3 dir = disney_sample(hd, C, u01(rn.x), u01(rn.y), u01(rn.z));
+        float r1 = u01(rn.w);
+        // shade, kernel.cu:339-358
+        f3 f = disney_eval(hd, C, dir);
+        float brdfPdf = disney_pdf(C, dir);
+        float ndl = fabsf(dot(dir, hd.normal));
+        // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked)
+        const DevTex& E = S.env;
+        int32_t cnt = hdri_search(S.cdf, r1, E.w * E.h);
+        float nu = __fdiv_rn((float)(cnt % E.w), (float)E.w), nv = __fdiv_rn((float)(cnt / E.w), (float)E.h);
+        int32_t ix = __float2int_rz(nu * (float)E.w), iy = __float2int_rz(nv * (float)E.h);
+        ix = __float2int_rz(E.x_tile * ((float)ix - E.x_offset * (float)E.w)) % E.w;
+        iy = __float2int_rz(E.y_tile * ((float)iy - E.y_offset * (float)E.h)) % E.h;
+        float iu = __fdiv_rn((float)ix, (float)E.w), iv = __fdiv_rn((float)iy, (float)E.h);
+        limit_uv(iu, iv);
+        f3 dH = -normalized(reverse_spherical(iu, iv));
+        float hdriPdf = hdri_pdf(S, __float2int_rz(iu * (float)E.w), __float2int_rz(iv * (float)E.h));
+        f3 eH = tex_uv(S, E, iu, iv);
+        f3 fH = disney_eval(hd, C, dH);
+        f3 hdriC = (fH * fabsf(dot(dH, hd.normal))) * eH / hdriPdf;
+        env_o = xadd(pos, xscale(dH, 0.001f));
+        env_d = xnormalize(dH);
+        push_env = true;
+        // point light NEE, kernel.cu:175-205
+        float pointPdf = 0.f;
+        f3 pointC = mk1(0.f);
+        if (S.n_lights > 0) {
+          pointPdf = (float)S.n_lights / (2.0f * ER_PI);
+          int32_t li = min(__float2int_rz((float)S.n_lights * r1), S.n_lights - 1);
+          const er_point_light& Lp = S.lights[li];
+          f3 lp = mk(Lp.position[0], Lp.position[1], Lp.position[2]);
+          f3 toL = xsub(lp, pos);
+          f3 dP = normalized(toL);
+          float dist = xlen(toL);
+          f3 fP = disney_eval(hd, C, dP);
+          f3 plv = mk(Lp.radiance[0], Lp.radiance[1], Lp.radiance[2]) / (dist * dist);
+          pointC = (plv * fP) * fabsf(dot(dP, hd.normal)) / pointPdf;
+          pt_o = xadd(pos, xscale(dP, 0.001f));
+          pt_d = xnormalize(dP);
+          pt_p = pos;
+          pt_dist = dist;
+          push_pt = true;
+        }
+        f3 brdfC = (f * ndl) * hd.emission / brdfPdf;
+        float den = hdriPdf + pointPdf + brdfPdf;
+        float w1 = hdriPdf / den, w2 = pointPdf / den, w3 = brdfPdf / den;
+        f3 tH = hdriC * w1, tP = pointC * w2, tB = brdfC * w3;
+        uint32_t fl = 1u | (push_pt ? 2u : 0u);
+        w.pend[4 * (size_t)p] = make_float4(tH.x, tH.y, tH.z, w1 * 0.0f);
+        w.pend[4 * (size_t)p + 1] = make_float4(tP.x, tP.y, tP.z, w2 * 0.0f);
+        w.pend[4 * (size_t)p + 2] = make_float4(tB.x, tB.y, tB.z, __uint_as_float(fl));
+        w.pend[4 * (size_t)p + 3] = make_float4(thr.x, thr.y, thr.z, 0.f);
+        f3 g = (f * ndl) / brdfPdf;
+        thr = mk(__fmul_rn(thr.x, g.x), __fmul_rn(thr.y, g.y), __fmul_rn(thr.z, g.z));
+        w.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
+        if (bounce == 0 && w.aov) {
+          w.aovs[3 * (size_t)p] = make_float4(sn.x, sn.y, sn.z, 0.f);
+          w.aovs[3 * (size_t)p + 1] = make_float4(tg.x, tg.y, tg.z, 0.f);
+          w.aovs[3 * (size_t)p + 2] = make_float4(bt.x, bt.y, bt.z, 0.f);
+        }
+        if (!last) {
+          // kernel.cu:442
+          next_o = xadd(pos, xscale(dir, 0.001f));
+          next_d = xnormalize(dir);
+          push_next = true;
+        }
+      }
+      w.light[p] = L;
+    }
+    int32_t j = warp_append(&w.counts[qout], push_next);
+    if (push_next) {
+      w.q_o[qout][j] = make_float4(next_o.x, next_o.y, next_o.z, __int_as_float(p));
+      w.q_d[qout][j] = make_float4(next_d.x, next_d.y, next_d.z, 0.f);
+    }
+    int32_t k = warp_append(&w.counts[2], push_env);
+    if (push_env) {
+      w.s_o[k] = make_float4(env_o.x, env_o.y, env_o.z, __int_as_float(2 * p));
+      w.s_d[k] = make_float4(env_d.x, env_d.y, env_d.z, 0.f);
+    }
+    k = warp_append(&w.counts[2], push_pt);
+    if (push_pt) {
+      w.s_o[k] = make_float4(pt_o.x, pt_o.y, pt_o.z, __int_as_float(2 * p + 1));
+      w.s_d[k] = make_float4(pt_d.x, pt_d.y, pt_d.z, pt_dist);
+      w.s_p[k] = make_float4(pt_p.x, pt_p.y, pt_p.z, 0.f);
+    }
+  }
+}
+
+// kernel.cu:445-478 per pixel, samples in index order.
+__global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw) {
+  int32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.npix) return;
+  int32_t x = pix % P.W, y = pix / P.W;
+  int32_t idx = out_index(P, x, y);
+  uint32_t sa = F.samples[idx], pc = F.pathcount[idx];
+  const bool fp64 = P.flags & ER_RENDER_ACCUM_FP64;
+  float4 bt = F.beauty[idx];
+  double s0 = 0, s1 = 0, s2 = 0;
+  if (fp64) { s0 = F.sum[3 * (size_t)idx]; s1 = F.sum[3 * (size_t)idx + 1]; s2 = F.sum[3 * (size_t)idx + 2]; }
+  float4 a[3];
+  if (F.aov_on) for (int k = 0; k < 3; k++) a[k] = F.aov[k][idx];
+  for (int32_t s = 0; s < sw; s++) {
+    int32_t p = s * P.npix + pix;
+    float4 L = w.light[p];
+    resolve(w, p, L);
+    pc += (uint32_t)w.bounces[p];
+    float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
+    if (isnan(lx) || isnan(ly) || isnan(lz)) continue;
+    float inv = __fadd_rn((float)sa, 1.0f);
+    if (fp64) {
+      s0 += lx; s1 += ly; s2 += lz;
+    } else {
+      if (sa > 0) {
+        float k = __fdiv_rn((float)sa, (float)(sa + 1));
+        bt.x = __fmul_rn(bt.x, k); bt.y = __fmul_rn(bt.y, k); bt.z = __fmul_rn(bt.z, k);
+      }
+      bt.x = __fadd_rn(bt.x, __fdiv_rn(lx, inv));
+      bt.y = __fadd_rn(bt.y, __fdiv_rn(ly, inv));
+      bt.z = __fadd_rn(bt.z, __fdiv_rn(lz, inv));
+    }
+    if (F.aov_on) {
+      for (int k = 0; k < 3; k++) {
+        float4 v = w.aov ? w.aovs[3 * (size_t)p + k] : make_float4(0, 0, 0, 0);
+        if (sa > 0) {
+          float kk = __fdiv_rn((float)sa, (float)(sa + 1));
+          a[k].x = __fmul_rn(a[k].x, kk); a[k].y = __fmul_rn(a[k].y, kk); a[k].z = __fmul_rn(a[k].z, kk);
+        }
+        a[k].x = __fadd_rn(a[k].x, __fdiv_rn(v.x, inv));
+        a[k].y = __fadd_rn(a[k].y, __fdiv_rn(v.y, inv));
+        a[k].z = __fadd_rn(a[k].z, __fdiv_rn(v.z, inv));
+      }
+    }
+    sa++;
+  }
+  if (fp64) {
+    F.sum[3 * (size_t)idx] = s0; F.sum[3 * (size_t)idx + 1] = s1; F.sum[3 * (size_t)idx + 2] = s2;
+    if (sa > 0) bt = make_float4((float)(s0 / sa), (float)(s1 / sa), (float)(s2 / sa), 1.0f);
+  }
+  F.beauty[idx] = bt;
+  if (F.aov_on) for (int k = 0; k < 3; k++) F.aov[k][idx] = a[k];
+  F.samples[idx] = sa;
+  F.pathcount[idx] = pc;
+}
+
+// Per-path dump for er_render_paths.
+__global__ void k_dump(WaveView w, WaveParams P, int32_t sw, float* rad, int32_t* bnc) {
+  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= sw * P.npix) return;
+  float4 L = w.light[p];
+  resolve(w, p, L);
+  int32_t pix = p % P.npix, s = p / P.npix;
+  int64_t j = (int64_t)s * P.npix + out_index(P, pix % P.W, pix / P.W);
+  rad[3 * j] = L.x; rad[3 * j + 1] = L.y; rad[3 * j + 2] = L.z;
+  bnc[j] = w.bounces[p];
+}
+
+__global__ void k_film_clear(Film F, int32_t npix) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  F.beauty[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+  if (F.aov_on) for (int k = 0; k < 3; k++) F.aov[k][i] = make_float4(0.f, 0.f, 0.f, 1.f);
+  if (F.sum) { F.sum[3 * (size_t)i] = 0; F.sum[3 * (size_t)i + 1] = 0; F.sum[3 * (size_t)i + 2] = 0; }
+  F.samples[i] = 0;
+  F.pathcount[i] = 0;
+}
+
+template <typename K>
+int grid_for(K kernel, int block, int sms) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, block, 0);
+  return std::max(1, nb) * sms;
+}
+
+er_status alloc_w(er_scene* s, Wave* w, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? ER_ERR_OOM : ER_ERR_CUDA, "wave buffer allocation failed");
+  }
+  w->mem.push_back(*p);
+  return ER_OK;
+}
+
+er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
+  if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov)) return ER_OK;
+  free_wave(s);
+  Wave* ww = new Wave();
+  s->wave = ww;
+  ww->cap = cap;
+  WaveView* w = &ww->v;
+  w->aov = aov;
+  w->stats = s->d_stats;
+  er_status st;
+#define AL(ptr, bytes) \
+  if ((st = alloc_w(s, ww, (void**)&(ptr), (bytes))) != ER_OK) { free_wave(s); return st; }
+  AL(w->thr, cap * sizeof(float4));
+  AL(w->light, cap * sizeof(float4));
+  AL(w->pend, 4 * cap * sizeof(float4));
+  AL(w->vis, 2 * cap);
+  AL(w->bounces, cap * sizeof(int32_t));
+  if (aov) AL(w->aovs, 3 * cap * sizeof(float4));
+  for (int q = 0; q < 2; q++) {
+    AL(w->q_o[q], cap * sizeof(float4));
+    AL(w->q_d[q], cap * sizeof(float4));
+  }
+  AL(w->hits, cap * sizeof(float4));
+  AL(w->s_o, 2 * cap * sizeof(float4));
+  AL(w->s_d, 2 * cap * sizeof(float4));
+  AL(w->s_p, 2 * cap * sizeof(float4));
+  AL(w->counts, 16 * sizeof(int32_t));
+#undef AL
+  return ER_OK;
+}
+
+er_status ensure_film(er_scene* s, bool aov, bool fp64, bool clear) {
+  Film& F = s->film;
+  int32_t W = s->camera.x_res, H = s->camera.y_res;
+  bool realloc = F.w != W || F.h != H || (aov && !F.aov_on) || (fp64 && !F.sum);
+  if (realloc) {
+    free_film(s);
+    F.w = W;
+    F.h = H;
+    size_t np = (size_t)W * H;
+    auto al = [&](void** p, size_t b) -> er_status {
+      cudaError_t e = cudaMalloc(p, b);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ER_ERR_OOM, "film allocation failed");
+      }
+      return ER_OK;
+    };
+    er_status st;
+    if ((st = al((void**)&F.beauty, np * sizeof(float4))) != ER_OK) return st;
+    if ((st = al((void**)&F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
+    if ((st = al((void**)&F.pathcount, np * sizeof(uint32_t))) != ER_OK) return st;
+    if (aov) {
+      for (int k = 0; k < 3; k++)
+        if ((st = al((void**)&F.aov[k], np * sizeof(float4))) != ER_OK) return st;
+      F.aov_on = true;
+    }
+    if (fp64 && (st = al((void**)&F.sum, np * 3 * sizeof(double))) != ER_OK) return st;
+    clear = true;
+  }
+  if (clear) {
+    int32_t npix = W * H;
+    k_film_clear<<<(npix + 255) / 256, 256, 0, s->stream>>>(F, npix);
+    ER_CUDA(cudaGetLastError());
+  }
+  return ER_OK;
+}
+
+er_status copy_out(er_scene* s, bool dev, void* dst, const void* src, size_t bytes) {
+  if (!dst) return ER_OK;
+  ER_CUDA(cudaMemcpyAsync(dst, src, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream));
+  return ER_OK;
+}
+
+// Runs the waves of one call.  dump_rad != null: single wave, per-path dump.
+er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* dump_b, int64_t* launches) {
+  const int32_t W = s->camera.x_res, H = s->camera.y_res;
+  const int32_t npix = W * H;
+  const bool aov = o->flags & ER_RENDER_AOV;
+  int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
+  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : std::max(1, (int32_t)((int64_t)(1 << 22) / npix));
+  sw = std::min(sw, std::max(1, o->spp));
+  if (dump_rad) sw = o->spp;
+  er_status st = ensure_wave(s, (int64_t)sw * npix, aov);
+  if (st != ER_OK) return st;
+  WaveView& w = s->wave->v;
+  WaveParams P;
+  P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
+  P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
+  P.flags = o->flags;
+  const bool q8 = s->dev.use_q8;
+  static int g_ext = 0, g_ext8 = 0, g_sh = 0, g_sh8 = 0, g_shade = 0;
+  if (!g_ext) {
+    g_ext = grid_for(k_extend<false>, kTravBlock, s->num_sms);
+    g_ext8 = grid_for(k_extend<true>, kTravBlock, s->num_sms);
+    g_sh = grid_for(k_shadow<false>, kTravBlock, s->num_sms);
+    g_sh8 = grid_for(k_shadow<true>, kTravBlock, s->num_sms);
+    g_shade = grid_for(k_shade, 128, s->num_sms);
+  }
+  int64_t nl = 0;
+  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+    int32_t cur = std::min(sw, o->spp - s0);
+    P.spp_wave = cur;
+    P.sample_base = o->sample_begin + s0;
+    int32_t n = cur * npix;
+    k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);
+    nl++;
+    int32_t q = 0;
+    for (int32_t b = 0; b < max_depth; b++) {
+      if (q8) k_extend<true><<<g_ext8, kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word);
+      else k_extend<false><<<g_ext, kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word);
+      k_shade<<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, q, b);
+      if (q8) k_shadow<true><<<g_sh8, kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word);
+      else k_shadow<false><<<g_sh, kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word);
+      nl += 3;
+      q ^= 1;
+    }
+    if (dump_rad) {
+      k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, dump_rad, dump_b);
+    } else {
+      Film F = s->film;
+      k_accumulate<<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur);
+    }
+    nl++;
+    ER_CUDA(cudaGetLastError());
+  }
+  if (launches) *launches = nl;
+  return ER_OK;
+}
+
+er_status check_opts(er_scene* s, const er_render_opts* o) {
+  if (!s || !o) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+  if (o->spp < 0 || o->sample_begin < 0 || o->max_depth < 0 || o->max_depth > 64 || o->spp_per_wave < 0)
+    return fail(ER_ERR_INVALID_ARG, "render options out of range");
+  ER_CUDA(cudaSetDevice(s->device));
+  return ER_OK;
+}
+
+}  // namespace
+
+void free_wave(er_scene* s) {
+  if (!s->wave) return;
+  for (void* p : s->wave->mem) cudaFree(p);
+  delete s->wave;
+  s->wave = nullptr;
+}
+
+void free_film(er_scene* s) {
+  Film& F = s->film;
+  cudaFree(F.beauty);
+  for (int k = 0; k < 3; k++) cudaFree(F.aov[k]);
+  cudaFree(F.sum);
+  cudaFree(F.samples);
+  cudaFree(F.pathcount);
+  F = Film();
+}
+
+}  // namespace er
+
+using namespace er;
+
+extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, float* normal, float* tangent,
+                                  float* bitangent, uint32_t* samples, uint32_t* pathcount) {
+  if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+  Film& F = s->film;
+  if (!F.beauty) return fail(ER_ERR_INVALID_ARG, "nothing rendered yet");
+  bool dev = flags & ER_RENDER_DEVICE_OUT;
+  size_t np = (size_t)F.w * F.h;
+  er_status st;
+  if ((st = copy_out(s, dev, beauty, F.beauty, np * sizeof(float4))) != ER_OK) return st;
+  float* aovs[3] = {normal, tangent, bitangent};
+  for (int k = 0; k < 3; k++) {
+    if (!aovs[k]) continue;
+    if (!F.aov_on) return fail(ER_ERR_INVALID_ARG, "AOV passes were not rendered");
+    if ((st = copy_out(s, dev, aovs[k], F.aov[k], np * sizeof(float4))) != ER_OK) return st;
+  }
+  if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
+  if ((st = copy_out(s, dev, pathcount, F.pathcount, np * sizeof(uint32_t))) != ER_OK) return st;
+  ER_CUDA(cudaStreamSynchronize(s->stream));
+  return ER_OK;
+}
+
+extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beauty, float* normal, float* tangent,
+                               float* bitangent, uint32_t* samples, uint32_t* pathcount, er_render_stats* stats) {
+  er_status st = check_opts(s, o);
+  if (st != ER_OK) return st;
+  const bool aov = o->flags & ER_RENDER_AOV;
+  const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
+  if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
+  unsigned long long st0[8];
+  ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
+  ER_CUDA(cudaEventRecord(s->ev0, s->stream));
+  int64_t launches = 0;
+  if ((st = run(s, o, nullptr, nullptr, &launches)) != ER_OK) return st;
+  ER_CUDA(cudaEventRecord(s->ev1, s->stream));
+  if (!(o->flags & ER_RENDER_NO_OUTPUT)) {
+    uint32_t fl = o->flags & ER_RENDER_DEVICE_OUT;
+    if ((st = er_film_read(s, fl, beauty, aov ? normal : nullptr, aov ? tangent : nullptr,
+                           aov ? bitangent : nullptr, samples, pathcount)) != ER_OK)
+      return st;
+  }
+  ER_CUDA(cudaEventSynchronize(s->ev1));
+  if ((st = check_device_error(s)) != ER_OK) return st;
+  if (stats) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    unsigned long long st1[8];
+    ER_CUDA(cudaMemcpy(st1, s->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
+    stats->ms = ms;
+    stats->samples = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
+    stats->rays_closest = (int64_t)(st1[0] - st0[0]);
+    stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
+    stats->path_vertices = 0;
+    stats->kernel_launches = launches;
+  }
+  return ER_OK;
+}
+
+extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float* radiance, int32_t* bounces) {
+  er_status st = check_opts(s, o);
+  if (st != ER_OK) return st;
+  if (!radiance || !bounces) return fail(ER_ERR_INVALID_ARG, "NULL output");
+  size_t n = (size_t)o->spp * s->camera.x_res * s->camera.y_res;
+  if (n == 0) return ER_OK;
+  float* d_rad = nullptr;
+  int32_t* d_b = nullptr;
+  if (cudaMalloc(&d_rad, n * 3 * sizeof(float)) != cudaSuccess || cudaMalloc(&d_b, n * sizeof(int32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d_rad);
+    return fail(ER_ERR_OOM, "path dump allocation failed");
+  }
+  er_render_opts oo = *o;
+  oo.flags &= ~(uint32_t)ER_RENDER_AOV;
+  st = run(s, &oo, d_rad, d_b, nullptr);
+  if (st == ER_OK) {
+    cudaMemcpyAsync(radiance, d_rad, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+    cudaMemcpyAsync(bounces, d_b, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "er_render_paths");
+  }
+  cudaFree(d_rad);
+  cudaFree(d_b);
+  if (st == ER_OK) st = check_device_error(s);
+  return st;
+}

@@ -1,0 +1,179 @@
+"""ctypes binding of libeleven.so (the product C-ABI, include/eleven.h).
+
+The library is built in-tree; loading fails loudly when it is missing or a
+call returns an error status.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_lib = None
+
+
+class ElevenError(RuntimeError):
+    def __init__(self, status, where, detail):
+        self.status = status
+        super().__init__(f"{where}: {A.STATUS_NAMES.get(status, status)}: {detail}")
+
+
+def lib_path():
+    from .build import LIB
+    return LIB
+
+
+def load(build_if_missing=True):
+    """Load libeleven.so, building it first if it is absent or stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if build_if_missing:
+        from . import build
+        build.build_product()
+    if not os.path.exists(path):
+        raise ElevenError(A.ER_ERR_UNSUPPORTED if hasattr(A, "ER_ERR_UNSUPPORTED") else 8, "load",
+                          f"{path} not built")
+    L = C.CDLL(path)
+    L.er_status_string.restype = C.c_char_p
+    L.er_status_string.argtypes = [A.er_status]
+    L.er_last_error.restype = C.c_char_p
+    L.er_abi_version.restype = C.c_int32
+    L.er_scene_create.restype = A.er_status
+    L.er_scene_create.argtypes = [C.POINTER(A.er_scene_desc), C.POINTER(A.er_scene_opts), C.POINTER(C.c_void_p)]
+    L.er_scene_load.restype = A.er_status
+    L.er_scene_load.argtypes = [C.c_char_p, C.POINTER(A.er_scene_opts), C.POINTER(C.c_void_p)]
+    L.er_scene_info_get.restype = A.er_status
+    L.er_scene_info_get.argtypes = [C.c_void_p, C.POINTER(A.er_scene_info)]
+    L.er_scene_set_camera.restype = A.er_status
+    L.er_scene_set_camera.argtypes = [C.c_void_p, C.POINTER(A.er_camera)]
+    L.er_scene_free.restype = A.er_status
+    L.er_scene_free.argtypes = [C.c_void_p]
+    L.er_render.restype = A.er_status
+    L.er_render.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(A.er_render_stats)]
+    L.er_film_read.restype = A.er_status
+    L.er_film_read.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p]
+    L.er_render_paths.restype = A.er_status
+    L.er_render_paths.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p]
+    L.er_trace_closest.restype = A.er_status
+    L.er_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_uint32, C.POINTER(A.er_trace_stats)]
+    L.er_encode_ldr.restype = A.er_status
+    L.er_encode_ldr.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+    L.er_write_image.restype = A.er_status
+    L.er_write_image.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != A.ER_OK:
+        raise ElevenError(status, where, load().er_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Scene:
+    """A scene handle on the GPU (er_scene)."""
+
+    def __init__(self, arrays=None, bvh_format=A.ER_BVH_FP32, max_leaf=0, device=0, stream=None, handle=None):
+        L = load()
+        self.arrays = arrays
+        if handle is not None:
+            self.h = handle
+            return
+        desc, keep = arrays.desc()
+        opts = A.er_scene_opts(bvh_format, max_leaf, device, stream)
+        h = C.c_void_p()
+        check(L.er_scene_create(C.byref(desc), C.byref(opts), C.byref(h)), "er_scene_create")
+        self.h = h
+
+    @classmethod
+    def load_folder(cls, path, bvh_format=A.ER_BVH_FP32):
+        L = load()
+        opts = A.er_scene_opts(bvh_format, 0, 0, None)
+        h = C.c_void_p()
+        check(L.er_scene_load(os.fsencode(path), C.byref(opts), C.byref(h)), "er_scene_load")
+        return cls(handle=h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().er_scene_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self):
+        i = A.er_scene_info()
+        check(load().er_scene_info_get(self.h, C.byref(i)), "er_scene_info_get")
+        return i
+
+    @property
+    def resolution(self):
+        cam = self.arrays.camera
+        return int(cam["x_res"]), int(cam["y_res"])
+
+    def trace(self, rays, normalize=True, stats=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = len(rays)
+        tri = np.zeros(n, np.int32)
+        dist = np.zeros(n, np.float32)
+        uv = np.zeros((n, 2), np.float32)
+        flags = (0 if normalize else A.ER_TRACE_NORMALIZED) | (A.ER_TRACE_STATS if stats else 0)
+        st = A.er_trace_stats()
+        check(load().er_trace_closest(self.h, _p(rays), n, _p(tri), _p(dist), _p(uv), flags, C.byref(st)),
+              "er_trace_closest")
+        return tri, dist, uv, st
+
+    def render(self, spp, max_depth=5, seed=0, sample_begin=0, spp_per_wave=0, flags=0, aov=False):
+        W, H = self.resolution
+        if aov:
+            flags |= A.ER_RENDER_AOV
+        o = A.er_render_opts(spp, sample_begin, max_depth, spp_per_wave, seed, flags, 0)
+        beauty = np.zeros((H * W, 4), np.float32)
+        aovs = [np.zeros((H * W, 4), np.float32) for _ in range(3)] if aov else [None] * 3
+        samples = np.zeros(H * W, np.uint32)
+        pc = np.zeros(H * W, np.uint32)
+        st = A.er_render_stats()
+        check(load().er_render(self.h, C.byref(o), _p(beauty), _p(aovs[0]), _p(aovs[1]), _p(aovs[2]),
+                               _p(samples), _p(pc), C.byref(st)), "er_render")
+        return dict(beauty=beauty, normal=aovs[0], tangent=aovs[1], bitangent=aovs[2], samples=samples,
+                    pathcount=pc, stats=st)
+
+    def render_paths(self, spp, max_depth=5, seed=0, sample_begin=0):
+        W, H = self.resolution
+        o = A.er_render_opts(spp, sample_begin, max_depth, 0, seed, 0, 0)
+        rad = np.zeros((spp, H * W, 3), np.float32)
+        b = np.zeros((spp, H * W), np.int32)
+        check(load().er_render_paths(self.h, C.byref(o), _p(rad), _p(b)), "er_render_paths")
+        return rad, b
+
+
+def encode_ldr(rgba, width, height):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(width * height * 4, np.uint8)
+    check(load().er_encode_ldr(_p(rgba), width, height, _p(out)), "er_encode_ldr")
+    return out
+
+
+def write_image(path, rgba_u8, width, height, as_bmp=False):
+    rgba_u8 = np.ascontiguousarray(rgba_u8, np.uint8)
+    check(load().er_write_image(os.fsencode(path), _p(rgba_u8), width, height, int(as_bmp)), "er_write_image")

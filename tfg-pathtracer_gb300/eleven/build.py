@@ -29,8 +29,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
-SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp", "image_io.cpp",
-           "trace.cu", "render.cu", "env.cu"]
+SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp",
+           "trace.cu", "render.cu"]
 
 
 def _run(cmd, cwd=None):

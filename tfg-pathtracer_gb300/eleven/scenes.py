@@ -222,31 +222,24 @@ def icosphere(subdiv):
 
 def uv_sphere(n_lat, n_lon):
     """Unit UV sphere with pole fans: 2*n_lon*(n_lat-1) triangles."""
-    th = np.linspace(0.0, np.pi, n_lat + 1)
+    th = np.linspace(0.0, np.pi, n_lat + 1)[1:-1]
     ph = np.linspace(0.0, 2 * np.pi, n_lon + 1)[:-1]
-    verts = [np.array([0.0, 1.0, 0.0])]
-    for i in range(1, n_lat):
-        s, c = np.sin(th[i]), np.cos(th[i])
-        verts += [np.array([s * np.cos(p), c, s * np.sin(p)]) for p in ph]
-    verts.append(np.array([0.0, -1.0, 0.0]))
-    verts = np.array(verts)
-    faces = []
-
-    def ring(i, j):
-        return 1 + (i - 1) * n_lon + (j % n_lon)
-
-    for j in range(n_lon):
-        faces.append((0, ring(1, j + 1), ring(1, j)))
-    for i in range(1, n_lat - 1):
-        for j in range(n_lon):
-            a, b = ring(i, j), ring(i, j + 1)
-            c, d = ring(i + 1, j), ring(i + 1, j + 1)
-            faces.append((a, b, d))
-            faces.append((a, d, c))
+    st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+    ring = np.stack([st * np.cos(ph)[None, :], np.broadcast_to(ct, (n_lat - 1, n_lon)),
+                     st * np.sin(ph)[None, :]], -1).reshape(-1, 3)
+    verts = np.concatenate([[[0.0, 1.0, 0.0]], ring, [[0.0, -1.0, 0.0]]])
     last = len(verts) - 1
-    for j in range(n_lon):
-        faces.append((last, ring(n_lat - 1, j), ring(n_lat - 1, j + 1)))
-    return verts, np.array(faces, dtype=np.int64)
+    j = np.arange(n_lon)
+    jn = (j + 1) % n_lon
+    top = np.stack([np.zeros(n_lon, np.int64), 1 + jn, 1 + j], 1)
+    i = np.arange(1, n_lat - 1)[:, None]
+    a = 1 + (i - 1) * n_lon + j[None, :]
+    b = 1 + (i - 1) * n_lon + jn[None, :]
+    c = 1 + i * n_lon + j[None, :]
+    d = 1 + i * n_lon + jn[None, :]
+    mid = np.stack([np.stack([a, b, d], -1), np.stack([a, d, c], -1)], 2).reshape(-1, 3)
+    bot = np.stack([np.full(n_lon, last), 1 + (n_lat - 2) * n_lon + j, 1 + (n_lat - 2) * n_lon + jn], 1)
+    return verts, np.concatenate([top, mid, bot]).astype(np.int64)
 
 
 def value_noise3(p, seed, octaves=1):
@@ -283,11 +276,30 @@ def _hash3(x, y, z, seed):
 
 
 def value_noise2_img(w, h, seed, octaves=4, cells=8):
-    """4-octave 2-D value noise image in [0,1], (h, w)."""
-    ys, xs = np.mgrid[0:h, 0:w]
-    p = np.stack([xs / w * cells, ys / h * cells, np.zeros_like(xs, dtype=np.float64)], -1).reshape(-1, 3)
-    n = value_noise3(p, seed, octaves)
-    return (0.5 + 0.5 * n).reshape(h, w)
+    """Octave value noise image in [0,1], (h, w): random lattice values,
+    smoothstep-interpolated, halving amplitude per octave."""
+    rng = np.random.default_rng(seed)
+    ys = (np.arange(h) + 0.5) / h
+    xs = (np.arange(w) + 0.5) / w
+    total = np.zeros((h, w))
+    amp, norm = 1.0, 0.0
+    for o in range(octaves):
+        n = cells * (2 ** o)
+        lat = rng.uniform(-1, 1, (n + 1, n + 1))
+        fy, fx = ys * n, xs * n
+        iy, ix = np.floor(fy).astype(np.int64), np.floor(fx).astype(np.int64)
+        ty, tx = fy - iy, fx - ix
+        ty, tx = ty * ty * (3 - 2 * ty), tx * tx * (3 - 2 * tx)
+        a = lat[iy][:, ix]
+        b = lat[iy][:, ix + 1]
+        c = lat[iy + 1][:, ix]
+        d = lat[iy + 1][:, ix + 1]
+        top = a + (b - a) * tx[None, :]
+        bot = c + (d - c) * tx[None, :]
+        total += amp * (top + (bot - top) * ty[:, None])
+        norm += amp
+        amp *= 0.5
+    return 0.5 + 0.5 * total / norm
 
 
 def vertex_normals(verts, faces):
