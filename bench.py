@@ -1,0 +1,332 @@
+"""Benchmark: Msamples/s of the Eleven Renderer sample path at 1080p on GB300.
+
+Workload (default): the full-feature scene -- 1920x1080, max depth 8,
+~1.18M triangles in 200 seeded displaced spheres, ten 512^2 value-noise
+baseColor textures, a 2048x1024 log-normal HDR environment with a sun patch,
+4 point lights, thin-lens camera (aperture 0.05, focus 10), MIS over all
+strategies.  Seeded synthetic data stands in for the reference's scenes.
+
+A step is one sample per pixel of the 1080p frame (2,073,600 path samples)
+through the wavefront tracer.  `value` is device-timed with CUDA events on
+the render stream, scene resident in HBM; `e2e` goes through the C-ABI call
+a user makes (er_render with host output buffers, the image read back every
+step).  The working set (BVH + triangles + textures + environment, ~0.2 GB,
+plus ~0.6 GB of queue traffic per step) exceeds the 126 MB L2, so no flush
+is inserted between steps.
+
+--impl reference times the reference's CPU path on the host cores: the
+oracle port of the reference (its depth-18 BVH, traversal and shading,
+restated in C), all host threads, a bounded pixel subset per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tfg-pathtracer_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Msamples/s at 1080p (plain wavefront, max depth 8)"
+UNIT = "Msamples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=128)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--bvh", default="fp32", choices=["fp32", "q8"])
+    ap.add_argument("--e2e-steps", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_scene(cfg):
+    from eleven import scenes
+    if cfg == "c0":
+        return scenes.config0(), 4, dict(workload="c0: 320x240 pinhole, 20,482 tris, 1 point light, constant env",
+                                         resolution="320x240", max_depth=4)
+    return scenes.config1(), 8, dict(
+        workload="c1: 1920x1080 thin lens, ~1.18M tris (200 displaced spheres), 10 textures 512^2, "
+                 "2048x1024 HDR env + sun, 4 point lights",
+        resolution="1920x1080", max_depth=8)
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier_max(pg, local, value):
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{local}")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg, local):
+    if pg is not None:
+        import torch
+        pg.barrier()
+        torch.cuda.synchronize(local)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_ray():
+    """DRAM bytes per traced ray of the dominant kernel from the committed ncu
+    summary (profiles/extend_c1_dram.json), or None."""
+    p = os.path.join(ROOT, "profiles", "extend_c1_dram.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
+def cpu_baseline(arrays, max_depth, seconds, seed=0):
+    """Oracle port of the reference on all host threads, bounded pixel subset."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    W, H = arrays.camera["x_res"], arrays.camera["y_res"]
+    orc = O.OrcScene(arrays)
+    cores = os.cpu_count() or 1
+    stride = 4096
+    t = time.perf_counter()
+    orc.render(spp=1, max_depth=max_depth, seed=seed, pixel_stride=stride)
+    dt = max(time.perf_counter() - t, 1e-3)
+    rate = ((W * H + stride - 1) // stride) / dt
+    stride = max(1, int(W * H / max(1.0, rate * seconds)))
+    n = (W * H + stride - 1) // stride
+    t = time.perf_counter()
+    r = orc.render(spp=1, max_depth=max_depth, seed=seed, pixel_stride=stride)
+    dt = time.perf_counter() - t
+    orc.close()
+    return dict(value=n / dt / 1e6, unit=UNIT, cores=cores, kind="port",
+                sample=f"1 spp on every {stride}th pixel of the 1080p frame ({n} samples, {dt:.1f} s, "
+                       f"{int(r['pathcount'].sum())} path vertices)"), dt
+
+
+def run_reference(args):
+    rank, world, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    arrays, max_depth, cfg = make_scene(args.config)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    W, H = arrays.camera["x_res"], arrays.camera["y_res"]
+    orc = O.OrcScene(arrays)
+    cores = os.cpu_count() or 1
+    # size one step to ~1.5 s of host work
+    t = time.perf_counter()
+    orc.render(spp=1, max_depth=max_depth, pixel_stride=4096)
+    rate = ((W * H + 4095) // 4096) / max(time.perf_counter() - t, 1e-3)
+    stride = max(1, int(W * H / max(1.0, rate * 1.5)))
+    n = (W * H + stride - 1) // stride
+    for i in range(args.warmup):
+        orc.render(spp=1, max_depth=max_depth, sample_begin=i, pixel_stride=stride)
+    t = time.perf_counter()
+    for i in range(args.steps):
+        orc.render(spp=1, max_depth=max_depth, sample_begin=args.warmup + i, pixel_stride=stride)
+    dt = time.perf_counter() - t
+    value = args.steps * n / dt / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, reference scene shapes)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"per step 1 spp on every {stride}th pixel ({n} samples)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    orc.close()
+    return 0
+
+
+def run_gpu(args):
+    from eleven import _abi as A
+    from eleven import _lib
+    rank, world, local, pg = dist_setup(args.gpus)
+    arrays, max_depth, cfg = make_scene(args.config)
+    W, H = arrays.camera["x_res"], arrays.camera["y_res"]
+    npix = W * H
+    fmt = A.ER_BVH_Q8 if args.bvh == "q8" else A.ER_BVH_FP32
+    scene = _lib.Scene(arrays, bvh_format=fmt, device=local)
+    info = scene.info()
+    base = rank * (args.warmup + args.steps + args.e2e_steps + 8)
+
+    # calibration (untimed): node visits / triangle tests per ray
+    cal = scene.render(spp=1, max_depth=max_depth, sample_begin=base,
+                       flags=A.ER_RENDER_COUNT | A.ER_RENDER_NO_OUTPUT)["stats"]
+    n_box_c = 4.0 * cal.closest_nodes / max(cal.rays_closest, 1)
+    n_tri_c = cal.closest_tris / max(cal.rays_closest, 1)
+    n_box_s = 4.0 * cal.shadow_nodes / max(cal.rays_shadow, 1)
+    n_tri_s = cal.shadow_tris / max(cal.rays_shadow, 1)
+    b_ray_c = 32 + 16 + 32 * n_box_c + 36 * n_tri_c
+    b_ray_s = 32 + 16 + 32 * n_box_s + 36 * n_tri_s
+
+    scene.render(spp=args.warmup, max_depth=max_depth, sample_begin=base + 1, flags=A.ER_RENDER_NO_OUTPUT)
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(pg, local)
+    t0 = time.perf_counter()
+    st = scene.render(spp=args.steps, max_depth=max_depth, sample_begin=base + 1 + args.warmup,
+                      flags=A.ER_RENDER_NO_OUTPUT | A.ER_RENDER_PROFILE)["stats"]
+    wall = time.perf_counter() - t0
+    ms = barrier_max(pg, local, st.ms)
+    clk = clocks.stop()
+    value = world * args.steps * npix / ms / 1e3
+
+    # e2e through the C-ABI with host buffers, one 1-spp call per step
+    beauty = np.zeros((npix, 4), np.float32)
+    samples = np.zeros(npix, np.uint32)
+    pathcount = np.zeros(npix, np.uint32)
+    import ctypes as C
+    L = _lib.load()
+    o = A.er_render_opts(1, 0, max_depth, 0, 0, 0, 0)
+    barrier(pg, local)
+    t0 = time.perf_counter()
+    for i in range(args.e2e_steps):
+        o.sample_begin = base + 2 + args.warmup + args.steps + i
+        o.flags = A.ER_RENDER_CONTINUE if i else 0
+        _lib.check(L.er_render(scene.h, C.byref(o), beauty.ctypes.data_as(C.c_void_p), None, None, None,
+                               samples.ctypes.data_as(C.c_void_p), pathcount.ctypes.data_as(C.c_void_p), None),
+                   "er_render")
+    e2e_s = barrier_max(pg, local, time.perf_counter() - t0)
+    e2e = world * args.e2e_steps * npix / e2e_s / 1e6
+    d2h = beauty.nbytes + samples.nbytes + pathcount.nbytes
+
+    # roofline of the dominant traversal kernel
+    ext_ms, sh_ms = st.stage_ms[1], st.stage_ms[3]
+    if sh_ms >= ext_ms:
+        kname, kms, rays, b_ray, nl = "k_shadow", sh_ms, st.rays_shadow, b_ray_s, st.stage_launches[3]
+    else:
+        kname, kms, rays, b_ray, nl = "k_extend", ext_ms, st.rays_closest, b_ray_c, st.stage_launches[1]
+    peak, peak_src = peaks()
+    achieved = rays * b_ray / (kms * 1e-3) / 1e9
+    tr = traffic_per_ray()
+    traffic = None
+    if tr and tr.get("kernel") == kname and args.config == tr.get("config"):
+        traffic = tr["dram_bytes_per_ray"] * rays / max(nl, 1)
+    stage = {n: round(st.stage_ms[k] / args.steps, 3) for k, n in enumerate(A.STAGES)}
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, reference scene shapes)",
+        "config": dict(cfg, spp_per_step=1, bvh=args.bvh, triangles=arrays.tri_count,
+                       l2="working set > 126 MB L2 (no flush)", parallelism="replicas" if world > 1 else "1 GPU"),
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(C.sizeof(A.er_render_opts)),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(st.kernel_launches),
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "algorithmic_bytes_per_ray": round(b_ray, 1),
+                     "launches": int(nl), "avg_launch_ms": round(kms / max(nl, 1), 4)},
+        "rays_per_s": {"closest": round(st.rays_closest / ms / 1e3, 1), "shadow": round(st.rays_shadow / ms / 1e3, 1),
+                       "unit": "Mrays/s"},
+        "path_vertices_per_s": round(st.path_vertices / ms / 1e3, 1),
+        "stage_ms_per_step": stage,
+        "per_ray": {"closest_box_tests": round(n_box_c, 2), "closest_tri_tests": round(n_tri_c, 2),
+                    "shadow_box_tests": round(n_box_s, 2), "shadow_tri_tests": round(n_tri_s, 2)},
+        "scene": {"bvh_build_ms": round(info.bvh_build_ms, 1), "upload_ms": round(info.upload_ms, 1),
+                  "nodes": int(info.node_count), "device_bytes": int(info.device_bytes)},
+        "wall_s_timed": round(wall, 3),
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb, _ = cpu_baseline(arrays, max_depth, args.cpu_seconds)
+        line["cpu_baseline"] = cb
+    scene.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -174,8 +174,14 @@ enum {
                                      texel distribution                     */
   ER_RENDER_CONTINUE = 1u << 4,   /* add samples to the film of the previous
                                      call instead of clearing it            */
-  ER_RENDER_NO_OUTPUT = 1u << 5   /* render into the film only              */
+  ER_RENDER_NO_OUTPUT = 1u << 5,  /* render into the film only              */
+  ER_RENDER_PROFILE = 1u << 6,    /* CUDA-event time per stage (stats)      */
+  ER_RENDER_COUNT = 1u << 7       /* count node visits / triangle tests     */
 };
+
+/* Stages of the wavefront, indices of er_render_stats.stage_ms */
+enum { ER_STAGE_RAYGEN = 0, ER_STAGE_EXTEND = 1, ER_STAGE_SHADE = 2, ER_STAGE_SHADOW = 3,
+       ER_STAGE_ACCUMULATE = 4, ER_STAGE_COUNT = 5 };
 
 typedef struct er_render_opts {
   int32_t spp;            /* samples per pixel of this call                 */
@@ -192,8 +198,13 @@ typedef struct er_render_stats {
   int64_t samples;        /* path samples traced                            */
   int64_t rays_closest;   /* extension rays traced                          */
   int64_t rays_shadow;    /* shadow rays traced                             */
-  int64_t path_vertices;  /* Σ bounce counts = reference "paths" counter    */
+  int64_t path_vertices;  /* sum of bounce counts: the reference's "paths"
+                             counter (kernel.cu:445, main.cpp:105-106)      */
   int64_t kernel_launches;
+  double stage_ms[ER_STAGE_COUNT];        /* with ER_RENDER_PROFILE        */
+  int64_t stage_launches[ER_STAGE_COUNT];
+  int64_t closest_nodes, closest_tris;    /* with ER_RENDER_COUNT          */
+  int64_t shadow_nodes, shadow_tris;
 } er_render_stats;
 
 /* Render `opts->spp` samples per pixel.  beauty (and, with ER_RENDER_AOV,

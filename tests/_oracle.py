@@ -41,6 +41,8 @@ def orc():
         _orc.orc_render.argtypes = [C.c_void_p, C.c_void_p, A.FP, A.FP, A.FP, A.FP, A.UP, A.UP]
         _orc.orc_render_paths.argtypes = [C.c_void_p, C.c_void_p, A.FP, A.IP]
         _orc.orc_encode_ldr.argtypes = [A.FP, C.c_int64, C.POINTER(C.c_uint8)]
+        _orc.orc_fastpow.restype = C.c_double
+        _orc.orc_fastpow.argtypes = [C.c_double, C.c_double]
         _orc.orc_u01.restype = C.c_float
         _orc.orc_u01.argtypes = [C.c_uint32]
         _bind_probes(_orc, "orc_p_")

@@ -1,0 +1,97 @@
+"""The C-ABI library loads, exports every symbol include/eleven.h declares,
+agrees with the ctypes mirror on struct layouts, and rejects bad arguments
+before touching a device."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from eleven import _abi as A
+from eleven import _lib, scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "eleven.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(er_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_and_exports_agree():
+    decl = declared_functions()
+    assert sorted(A.EXPORTED) == decl
+    L = _lib.load()
+    for name in decl:
+        assert hasattr(L, name), name
+
+
+def test_library_exports_in_symbol_table():
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.lib_path()], capture_output=True, text=True).stdout
+    syms = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    for name in declared_functions():
+        assert name in syms, name
+
+
+STRUCTS = ["er_camera", "er_material", "er_texture", "er_point_light", "er_scene_desc", "er_scene_opts",
+           "er_scene_info", "er_render_opts", "er_render_stats", "er_trace_stats"]
+
+
+def test_struct_layouts(tmp_path):
+    prog = tmp_path / "sz.c"
+    body = "".join(f'printf("{s} %zu\\n", sizeof({s}));' for s in STRUCTS)
+    prog.write_text(f'#include <stdio.h>\n#include "eleven.h"\nint main(void){{{body}return 0;}}\n')
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)], check=True)
+    sizes = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    for s in STRUCTS:
+        assert int(sizes[s]) == C.sizeof(getattr(A, s)), s
+
+
+def test_status_strings_and_version():
+    L = _lib.load()
+    assert L.er_abi_version() == 1
+    for code in range(10):
+        assert L.er_status_string(code)
+    assert L.er_status_string(12345) == b"unknown status"
+
+
+def test_invalid_arguments_rejected():
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.er_scene_create(None, None, C.byref(h)) == A.ER_ERR_INVALID_ARG
+    assert L.er_last_error()
+    arr = scenes.config0(8, 6, n_spheres=1, subdiv=0)
+    arr.positions = arr.positions.copy()
+    arr.positions[0, 0, 0] = np.nan
+    d, keep = arr.desc()
+    assert L.er_scene_create(C.byref(d), None, C.byref(h)) == 1
+    arr = scenes.config0(8, 6, n_spheres=1, subdiv=0)
+    arr.object_material = np.full_like(arr.object_material, 99)
+    d, keep = arr.desc()
+    assert L.er_scene_create(C.byref(d), None, C.byref(h)) == 1
+    assert b"object_material" in L.er_last_error()
+    arr = scenes.config0(0, 6, n_spheres=1, subdiv=0)
+    d, keep = arr.desc()
+    assert L.er_scene_create(C.byref(d), None, C.byref(h)) == 1
+    assert L.er_scene_free(None) == 0
+    assert L.er_trace_closest(None, None, 0, None, None, None, 0, None) == 1
+    assert L.er_render(None, None, None, None, None, None, None, None, None) == 1
+
+
+def test_no_device_is_reported_not_faked():
+    """Without a GPU the library reports it; there is no CPU fallback."""
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(_lib.ElevenError) as e:
+        _lib.Scene(scenes.config0(8, 6, n_spheres=1, subdiv=0))
+    assert e.value.status == 9

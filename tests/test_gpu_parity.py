@@ -45,6 +45,21 @@ def test_closest_ids_random_rays(c0):
     assert (tri >= 0).sum() > 10_000
 
 
+def test_closest_ids_vs_reference_golden():
+    """GPU hit IDs against the reference's own BVH::transverse outputs
+    (host-compiled reference headers, tests/golden/reference_vectors.npz)."""
+    from test_oracle_golden import GOLD, golden_scene
+    G = dict(np.load(GOLD))
+    scene = _lib.Scene(golden_scene(G))
+    tri, dist, _, _ = scene.trace(G["trace_rays"])
+    bad = np.nonzero(tri != G["trace_tri"])[0]
+    ties = [i for i in bad if dist[i] == G["trace_dist"][i]]
+    assert len(bad) == len(ties), f"{len(bad) - len(ties)} non-tie mismatches"
+    ok = tri == G["trace_tri"]
+    assert np.array_equal(dist[ok].view(np.uint32), G["trace_dist"][ok].view(np.uint32))
+    scene.close()
+
+
 def test_closest_ids_camera_rays(c0):
     """Primary rays generated on the GPU, traced on both sides."""
     arrays, scene, orc = c0

@@ -155,6 +155,8 @@ struct er_scene {
   er::Wave* wave = nullptr;
   uint32_t* err_word = nullptr;   // device error word (bounds / timeout)
   unsigned long long* d_stats = nullptr;  // device ray counters
+  std::vector<cudaEvent_t> ev_pool;       // per-launch profiling events
+  std::vector<int> ev_stage;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 

@@ -101,7 +101,21 @@ __global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n) {
   }
 }
 
-template <bool Q8>
+// Adds per-thread traversal counters into stats[k], stats[k+1] (one atomic
+// per warp).
+__device__ __forceinline__ void flush_counts(unsigned long long* stats, int k, const TravStats& st) {
+  unsigned long long a = st.nodes, b = st.tris;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xFFFFFFFFu, a, o);
+    b += __shfl_down_sync(0xFFFFFFFFu, b, o);
+  }
+  if (lane_id() == 0) {
+    atomicAdd(&stats[k], a);
+    atomicAdd(&stats[k + 1], b);
+  }
+}
+
+template <bool Q8, bool STATS>
 __global__ void __launch_bounds__(kTravBlock) k_extend(DevScene S, WaveView w, int32_t qin, uint32_t* err) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -115,13 +129,14 @@ __global__ void __launch_bounds__(kTravBlock) k_extend(DevScene S, WaveView w, i
   TravStats st{0, 0, 0};
   for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 a = qo[i], b = qd[i];
-    TravResult r = traverse<kClosest, Q8, false>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk1(0.f), 0.f,
+    TravResult r = traverse<kClosest, Q8, STATS>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk1(0.f), 0.f,
                                                  stk + threadIdx.x, st, err);
     w.hits[i] = make_float4(r.t, r.u, r.v, __int_as_float(r.slot));
   }
+  if (STATS) flush_counts(w.stats, 2, st);
 }
 
-template <bool Q8>
+template <bool Q8, bool STATS>
 __global__ void __launch_bounds__(kTravBlock) k_shadow(DevScene S, WaveView w, uint32_t* err) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[1], (unsigned long long)w.counts[2]);
@@ -134,12 +149,13 @@ __global__ void __launch_bounds__(kTravBlock) k_shadow(DevScene S, WaveView w, u
     bool occ;
     if (tag & 1) {
       float4 q = w.s_p[i];
-      occ = traverse<kPoint, Q8, false>(S, o, d, mk(q.x, q.y, q.z), b.w, stk + threadIdx.x, st, err).occluded;
+      occ = traverse<kPoint, Q8, STATS>(S, o, d, mk(q.x, q.y, q.z), b.w, stk + threadIdx.x, st, err).occluded;
     } else {
-      occ = traverse<kAny, Q8, false>(S, o, d, mk1(0.f), 0.f, stk + threadIdx.x, st, err).occluded;
+      occ = traverse<kAny, Q8, STATS>(S, o, d, mk1(0.f), 0.f, stk + threadIdx.x, st, err).occluded;
     }
     w.vis[tag] = occ ? 0 : 1;  // tag = 2*path + type
   }
+  if (STATS) flush_counts(w.stats, 4, st);
 }
 
 // Resolve the pending MIS terms of a path's last shaded vertex
@@ -335,9 +351,21 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
 }
 
 // kernel.cu:445-478 per pixel, samples in index order.
+__device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WaveParams& P, const Film& F, int32_t sw,
+                                                 int32_t pix, uint32_t& bounce_sum);
+
 __global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw) {
   int32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= P.npix) return;
+  uint32_t bsum = 0;
+  if (pix < P.npix) accumulate_pixel(w, P, F, sw, pix, bsum);
+  // path-vertex counter (the reference's kPaths numerator), one atomic per warp
+  unsigned long long v = bsum;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if (lane_id() == 0 && v) atomicAdd(&w.stats[6], v);
+}
+
+__device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WaveParams& P, const Film& F, int32_t sw,
+                                                 int32_t pix, uint32_t& bounce_sum) {
   int32_t x = pix % P.W, y = pix / P.W;
   int32_t idx = out_index(P, x, y);
   uint32_t sa = F.samples[idx], pc = F.pathcount[idx];
@@ -352,6 +380,7 @@ __global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw) {
     float4 L = w.light[p];
     resolve(w, p, L);
     pc += (uint32_t)w.bounces[p];
+    bounce_sum += (uint32_t)w.bounces[p];
     float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
     if (isnan(lx) || isnan(ly) || isnan(lz)) continue;
     float inv = __fadd_rn((float)sa, 1.0f);
@@ -520,30 +549,70 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
   P.flags = o->flags;
   const bool q8 = s->dev.use_q8;
-  static int g_ext = 0, g_ext8 = 0, g_sh = 0, g_sh8 = 0, g_shade = 0;
-  if (!g_ext) {
-    g_ext = grid_for(k_extend<false>, kTravBlock, s->num_sms);
-    g_ext8 = grid_for(k_extend<true>, kTravBlock, s->num_sms);
-    g_sh = grid_for(k_shadow<false>, kTravBlock, s->num_sms);
-    g_sh8 = grid_for(k_shadow<true>, kTravBlock, s->num_sms);
+  const bool count = o->flags & ER_RENDER_COUNT;
+  const bool prof = o->flags & ER_RENDER_PROFILE;
+  static int g_ext[4] = {0}, g_sh[4] = {0}, g_shade = 0;
+  if (!g_shade) {
+    g_ext[0] = grid_for(k_extend<false, false>, kTravBlock, s->num_sms);
+    g_ext[1] = grid_for(k_extend<true, false>, kTravBlock, s->num_sms);
+    g_ext[2] = grid_for(k_extend<false, true>, kTravBlock, s->num_sms);
+    g_ext[3] = grid_for(k_extend<true, true>, kTravBlock, s->num_sms);
+    g_sh[0] = grid_for(k_shadow<false, false>, kTravBlock, s->num_sms);
+    g_sh[1] = grid_for(k_shadow<true, false>, kTravBlock, s->num_sms);
+    g_sh[2] = grid_for(k_shadow<false, true>, kTravBlock, s->num_sms);
+    g_sh[3] = grid_for(k_shadow<true, true>, kTravBlock, s->num_sms);
     g_shade = grid_for(k_shade, 128, s->num_sms);
   }
+  const int variant = (q8 ? 1 : 0) + (count ? 2 : 0);
   int64_t nl = 0;
+  // Profiling: one event after every launch, attributed to its stage.
+  s->ev_stage.clear();
+  auto mark = [&](int stage) -> er_status {
+    nl++;
+    if (!prof) return ER_OK;
+    size_t k = s->ev_stage.size() + 1;
+    while (s->ev_pool.size() <= k) {
+      cudaEvent_t e;
+      ER_CUDA(cudaEventCreate(&e));
+      s->ev_pool.push_back(e);
+    }
+    ER_CUDA(cudaEventRecord(s->ev_pool[k], s->stream));
+    s->ev_stage.push_back(stage);
+    return ER_OK;
+  };
+  if (prof) {
+    if (s->ev_pool.empty()) {
+      cudaEvent_t e;
+      ER_CUDA(cudaEventCreate(&e));
+      s->ev_pool.push_back(e);
+    }
+    ER_CUDA(cudaEventRecord(s->ev_pool[0], s->stream));
+  }
   for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
     int32_t cur = std::min(sw, o->spp - s0);
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * npix;
     k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);
-    nl++;
+    if ((st = mark(ER_STAGE_RAYGEN)) != ER_OK) return st;
     int32_t q = 0;
     for (int32_t b = 0; b < max_depth; b++) {
-      if (q8) k_extend<true><<<g_ext8, kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word);
-      else k_extend<false><<<g_ext, kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word);
+      switch (variant) {
+        case 0: k_extend<false, false><<<g_ext[0], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
+        case 1: k_extend<true, false><<<g_ext[1], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
+        case 2: k_extend<false, true><<<g_ext[2], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
+        default: k_extend<true, true><<<g_ext[3], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
+      }
+      if ((st = mark(ER_STAGE_EXTEND)) != ER_OK) return st;
       k_shade<<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, q, b);
-      if (q8) k_shadow<true><<<g_sh8, kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word);
-      else k_shadow<false><<<g_sh, kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word);
-      nl += 3;
+      if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
+      switch (variant) {
+        case 0: k_shadow<false, false><<<g_sh[0], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
+        case 1: k_shadow<true, false><<<g_sh[1], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
+        case 2: k_shadow<false, true><<<g_sh[2], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
+        default: k_shadow<true, true><<<g_sh[3], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
+      }
+      if ((st = mark(ER_STAGE_SHADOW)) != ER_OK) return st;
       q ^= 1;
     }
     if (dump_rad) {
@@ -552,7 +621,7 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
       Film F = s->film;
       k_accumulate<<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur);
     }
-    nl++;
+    if ((st = mark(ER_STAGE_ACCUMULATE)) != ER_OK) return st;
     ER_CUDA(cudaGetLastError());
   }
   if (launches) *launches = nl;
@@ -637,12 +706,23 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     unsigned long long st1[8];
     ER_CUDA(cudaMemcpy(st1, s->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
+    std::memset(stats, 0, sizeof *stats);
     stats->ms = ms;
     stats->samples = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
     stats->rays_closest = (int64_t)(st1[0] - st0[0]);
     stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
-    stats->path_vertices = 0;
+    stats->closest_nodes = (int64_t)(st1[2] - st0[2]);
+    stats->closest_tris = (int64_t)(st1[3] - st0[3]);
+    stats->shadow_nodes = (int64_t)(st1[4] - st0[4]);
+    stats->shadow_tris = (int64_t)(st1[5] - st0[5]);
+    stats->path_vertices = (int64_t)(st1[6] - st0[6]);
     stats->kernel_launches = launches;
+    for (size_t k = 0; k < s->ev_stage.size(); k++) {
+      float e = 0;
+      cudaEventElapsedTime(&e, s->ev_pool[k], s->ev_pool[k + 1]);
+      stats->stage_ms[s->ev_stage[k]] += e;
+      stats->stage_launches[s->ev_stage[k]]++;
+    }
   }
   return ER_OK;
 }

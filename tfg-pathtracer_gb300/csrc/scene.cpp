@@ -370,6 +370,7 @@ extern "C" er_status er_scene_free(er_scene* s) {
   free_film(s);
   for (void* p : s->allocs) cudaFree(p);
   s->allocs.clear();
+  for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);

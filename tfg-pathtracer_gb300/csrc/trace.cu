@@ -26,9 +26,9 @@ __global__ void __launch_bounds__(kTravBlock)
     }
   }
   if (STATS) {
-    atomicAdd(&stats[2], (unsigned long long)st.nodes);
-    atomicAdd(&stats[3], (unsigned long long)st.boxes);
-    atomicAdd(&stats[4], (unsigned long long)st.tris);
+    atomicAdd(&stats[8], (unsigned long long)st.nodes);
+    atomicAdd(&stats[9], (unsigned long long)st.boxes);
+    atomicAdd(&stats[10], (unsigned long long)st.tris);
   }
 }
 
@@ -83,7 +83,7 @@ extern "C" er_status er_trace_closest(er_scene* s, const float* rays, int64_t n,
     d_uv = (float*)e;
     cudaMemcpyAsync(a, rays, (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice, s->stream);
   }
-  unsigned long long s0[8] = {0};
+  unsigned long long s0[16] = {0};
   if (want_stats) cudaMemcpyAsync(s0, s->d_stats, sizeof s0, cudaMemcpyDeviceToHost, s->stream);
   cudaEventRecord(s->ev0, s->stream);
   int norm = (flags & ER_TRACE_NORMALIZED) ? 0 : 1;
@@ -116,11 +116,11 @@ extern "C" er_status er_trace_closest(er_scene* s, const float* rays, int64_t n,
     stats->ms = ms;
     stats->node_visits = stats->box_tests = stats->tri_tests = 0;
     if (want_stats) {
-      unsigned long long s1[8];
+      unsigned long long s1[16];
       cudaMemcpy(s1, s->d_stats, sizeof s1, cudaMemcpyDeviceToHost);
-      stats->node_visits = (int64_t)(s1[2] - s0[2]);
-      stats->box_tests = (int64_t)(s1[3] - s0[3]);
-      stats->tri_tests = (int64_t)(s1[4] - s0[4]);
+      stats->node_visits = (int64_t)(s1[8] - s0[8]);
+      stats->box_tests = (int64_t)(s1[9] - s0[9]);
+      stats->tri_tests = (int64_t)(s1[10] - s0[10]);
     }
   }
   return ER_OK;

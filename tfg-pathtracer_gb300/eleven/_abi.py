@@ -8,6 +8,15 @@ import ctypes as C
 er_status = C.c_int32
 
 ER_OK = 0
+ER_ERR_INVALID_ARG = 1
+ER_ERR_IO = 2
+ER_ERR_PARSE = 3
+ER_ERR_CUDA = 4
+ER_ERR_OOM = 5
+ER_ERR_DEVICE_CHECK = 6
+ER_ERR_TIMEOUT = 7
+ER_ERR_UNSUPPORTED = 8
+ER_ERR_NO_DEVICE = 9
 STATUS_NAMES = {
     0: "ER_OK", 1: "ER_ERR_INVALID_ARG", 2: "ER_ERR_IO", 3: "ER_ERR_PARSE",
     4: "ER_ERR_CUDA", 5: "ER_ERR_OOM", 6: "ER_ERR_DEVICE_CHECK",
@@ -112,11 +121,19 @@ class er_render_opts(C.Structure):
     ]
 
 
+ER_RENDER_PROFILE = 1 << 6
+ER_RENDER_COUNT = 1 << 7
+STAGES = ["raygen", "extend", "shade", "shadow", "accumulate"]
+
+
 class er_render_stats(C.Structure):
     _fields_ = [
         ("ms", C.c_double), ("samples", C.c_int64),
         ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64),
         ("path_vertices", C.c_int64), ("kernel_launches", C.c_int64),
+        ("stage_ms", C.c_double * 5), ("stage_launches", C.c_int64 * 5),
+        ("closest_nodes", C.c_int64), ("closest_tris", C.c_int64),
+        ("shadow_nodes", C.c_int64), ("shadow_tris", C.c_int64),
     ]
 
 
