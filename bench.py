@@ -270,14 +270,13 @@ def run_gpu(args):
     e2e = world * args.e2e_steps * npix / e2e_s / 1e6
     d2h = beauty.nbytes + samples.nbytes + pathcount.nbytes
 
-    # roofline of the dominant traversal kernel
-    ext_ms, sh_ms = st.stage_ms[1], st.stage_ms[3]
-    if sh_ms >= ext_ms:
-        kname, kms, rays, b_ray, nl = "k_shadow", sh_ms, st.rays_shadow, b_ray_s, st.stage_launches[3]
-    else:
-        kname, kms, rays, b_ray, nl = "k_extend", ext_ms, st.rays_closest, b_ray_c, st.stage_launches[1]
+    # roofline of the dominant kernel: k_trace (extension + shadow rays)
+    kname, kms, nl = "k_trace", st.stage_ms[1], st.stage_launches[1]
+    rays = st.rays_closest + st.rays_shadow
+    alg_bytes = st.rays_closest * b_ray_c + st.rays_shadow * b_ray_s
+    b_ray = alg_bytes / max(rays, 1)
     peak, peak_src = peaks()
-    achieved = rays * b_ray / (kms * 1e-3) / 1e9
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
     tr = traffic_per_ray()
     traffic = None
     if tr and tr.get("kernel") == kname and args.config == tr.get("config"):

@@ -179,8 +179,10 @@ enum {
   ER_RENDER_COUNT = 1u << 7       /* count node visits / triangle tests     */
 };
 
-/* Stages of the wavefront, indices of er_render_stats.stage_ms */
-enum { ER_STAGE_RAYGEN = 0, ER_STAGE_EXTEND = 1, ER_STAGE_SHADE = 2, ER_STAGE_SHADOW = 3,
+/* Stages of the wavefront, indices of er_render_stats.stage_ms.  TRACE is
+ * the traversal launch of a bounce (its extension rays together with the
+ * previous bounce's shadow rays); index 3 is reserved. */
+enum { ER_STAGE_RAYGEN = 0, ER_STAGE_TRACE = 1, ER_STAGE_SHADE = 2, ER_STAGE_RESERVED = 3,
        ER_STAGE_ACCUMULATE = 4, ER_STAGE_COUNT = 5 };
 
 typedef struct er_render_opts {

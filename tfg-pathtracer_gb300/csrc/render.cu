@@ -34,8 +34,9 @@ struct WaveView {
   float4* s_o = nullptr;
   float4* s_d = nullptr;
   float4* s_p = nullptr;
-  int32_t* counts = nullptr;       // [0],[1] extension queues, [2] shadow queue
+  int32_t* counts = nullptr;       // queue sizes and claim counters (see k_extend)
   unsigned long long* stats = nullptr;  // [0] closest rays [1] shadow rays (owned by the scene)
+  int64_t shadow_half = 0;         // point-light rays start here in the shadow queue
 };
 
 struct Wave {
@@ -49,6 +50,15 @@ struct WaveParams {
   uint32_t k0, k1;
   uint32_t flags;
 };
+
+// Queue counters (w.counts), by bounce parity q = b & 1:
+//   kExt + q      extension rays of bounce b (written by raygen / shade(b-1))
+//   kEnv + q      env shadow rays of bounce b (written by shade(b))
+//   kPt + q       point-light shadow rays of bounce b (written by shade(b))
+//   kClaim + 0..2 claim counters of the trace kernel's three phases
+// Each count is zeroed by a kernel that runs after its last reader and
+// before its first writer.
+constexpr int kExt = 0, kEnv = 2, kPt = 4, kClaim = 8;
 
 namespace {
 
@@ -75,9 +85,8 @@ __device__ __forceinline__ int32_t out_index(const WaveParams& P, int32_t x, int
 __global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p == 0) {
-    w.counts[0] = n;
-    w.counts[1] = 0;
-    w.counts[2] = 0;
+    for (int k = 0; k < 16; k++) w.counts[k] = 0;
+    w.counts[kExt] = n;
   }
   if (p >= n) return;
   int32_t pix = p % P.npix, s = p / P.npix;
@@ -115,47 +124,59 @@ __device__ __forceinline__ void flush_counts(unsigned long long* stats, int k, c
   }
 }
 
+// One traversal launch per bounce: the extension rays of bounce b (closest
+// hit) together with the shadow rays of bounce b-1, which are independent
+// of them.  Three persistent phases; every warp helps in all of them.
 template <bool Q8, bool STATS>
-__global__ void __launch_bounds__(kTravBlock) k_extend(DevScene S, WaveView w, int32_t qin, uint32_t* err) {
+__global__ void __launch_bounds__(kTravBlock, kTravMinBlocks) k_trace(DevScene S, WaveView w, int32_t b, uint32_t* err) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
+  const int32_t q = b & 1, qp = q ^ 1;
+  const int32_t n_ext = w.counts[kExt + q];
+  const int32_t n_pt = w.counts[kPt + qp];
+  const int32_t n_env = w.counts[kEnv + qp];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    w.counts[qin ^ 1] = 0;
-    w.counts[2] = 0;
-    atomicAdd(&w.stats[0], (unsigned long long)w.counts[qin]);
+    w.counts[kExt + qp] = 0;  // shade(b) appends the next extension rays
+    w.counts[kEnv + q] = 0;   // ... and the shadow rays of bounce b
+    w.counts[kPt + q] = 0;
+    atomicAdd(&w.stats[0], (unsigned long long)n_ext);
+    atomicAdd(&w.stats[1], (unsigned long long)(n_env + n_pt));
   }
-  const int32_t n = w.counts[qin];
-  const float4* qo = w.q_o[qin];
-  const float4* qd = w.q_d[qin];
-  TravStats st{0, 0, 0};
-  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 a = qo[i], b = qd[i];
-    TravResult r = traverse<kClosest, Q8, STATS>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk1(0.f), 0.f,
-                                                 stk + threadIdx.x, st, err);
-    w.hits[i] = make_float4(r.t, r.u, r.v, __int_as_float(r.slot));
+  const float4* qo = w.q_o[q];
+  const float4* qd = w.q_d[q];
+  float4* hits = w.hits;
+  const float4* so = w.s_o;
+  const float4* sd = w.s_d;
+  const float4* spp = w.s_p;
+  uint8_t* vis = w.vis;
+  const int64_t half = w.shadow_half;
+  TravStats st{0, 0, 0}, ss{0, 0, 0};
+  persistent_traverse<kClosest, Q8, STATS>(
+      S, n_ext, &w.counts[kClaim], stk + threadIdx.x, st, err,
+      [&](int32_t i, auto& tr) {
+        float4 a = qo[i], d = qd[i];
+        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+      },
+      [&](int32_t i, auto& tr) { hits[i] = make_float4(tr.t, tr.u, tr.v, __int_as_float(tr.slot)); });
+  // point-light rays: shadow queue [half, half + n_pt)
+  persistent_traverse<kPoint, Q8, STATS>(
+      S, n_pt, &w.counts[kClaim + 1], stk + threadIdx.x, ss, err,
+      [&](int32_t i, auto& tr) {
+        float4 a = so[half + i], d = sd[half + i], p = spp[half + i];
+        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk(p.x, p.y, p.z), d.w);
+      },
+      [&](int32_t i, auto& tr) { vis[__float_as_int(so[half + i].w)] = tr.occluded ? 0 : 1; });
+  // env rays: shadow queue [0, n_env)
+  persistent_traverse<kAny, Q8, STATS>(
+      S, n_env, &w.counts[kClaim + 2], stk + threadIdx.x, ss, err,
+      [&](int32_t i, auto& tr) {
+        float4 a = so[i], d = sd[i];
+        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+      },
+      [&](int32_t i, auto& tr) { vis[__float_as_int(so[i].w)] = tr.occluded ? 0 : 1; });
+  if (STATS) {
+    flush_counts(w.stats, 2, st);
+    flush_counts(w.stats, 4, ss);
   }
-  if (STATS) flush_counts(w.stats, 2, st);
-}
-
-template <bool Q8, bool STATS>
-__global__ void __launch_bounds__(kTravBlock) k_shadow(DevScene S, WaveView w, uint32_t* err) {
-  __shared__ int2 stk[kSmemStack * kTravBlock];
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[1], (unsigned long long)w.counts[2]);
-  const int32_t n = w.counts[2];
-  TravStats st{0, 0, 0};
-  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 a = w.s_o[i], b = w.s_d[i];
-    int32_t tag = __float_as_int(a.w);
-    f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
-    bool occ;
-    if (tag & 1) {
-      float4 q = w.s_p[i];
-      occ = traverse<kPoint, Q8, STATS>(S, o, d, mk(q.x, q.y, q.z), b.w, stk + threadIdx.x, st, err).occluded;
-    } else {
-      occ = traverse<kAny, Q8, STATS>(S, o, d, mk1(0.f), 0.f, stk + threadIdx.x, st, err).occluded;
-    }
-    w.vis[tag] = occ ? 0 : 1;  // tag = 2*path + type
-  }
-  if (STATS) flush_counts(w.stats, 4, st);
 }
 
 // Resolve the pending MIS terms of a path's last shaded vertex
@@ -178,11 +199,17 @@ __device__ __forceinline__ void resolve(const WaveView& w, int32_t p, float4& L)
   w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
 }
 
-__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParams P, int32_t qin, int32_t bounce) {
-  const int32_t n = w.counts[qin];
+__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParams P, int32_t bounce) {
+  const int32_t qin = bounce & 1;
+  const int32_t n = w.counts[kExt + qin];
   const float4* qo = w.q_o[qin];
   const float4* qd = w.q_d[qin];
   const int32_t qout = qin ^ 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counts[kClaim] = 0;  // the next trace launch claims from zero
+    w.counts[kClaim + 1] = 0;
+    w.counts[kClaim + 2] = 0;
+  }
   const bool last = bounce + 1 >= P.max_depth;
   for (int32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     int32_t i = base + threadIdx.x;
@@ -331,21 +358,22 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
       }
       w.light[p] = L;
     }
-    int32_t j = warp_append(&w.counts[qout], push_next);
+    int32_t j = warp_append(&w.counts[kExt + qout], push_next);
     if (push_next) {
       w.q_o[qout][j] = make_float4(next_o.x, next_o.y, next_o.z, __int_as_float(p));
       w.q_d[qout][j] = make_float4(next_d.x, next_d.y, next_d.z, 0.f);
     }
-    int32_t k = warp_append(&w.counts[2], push_env);
+    int32_t k = warp_append(&w.counts[kEnv + qin], push_env);
     if (push_env) {
       w.s_o[k] = make_float4(env_o.x, env_o.y, env_o.z, __int_as_float(2 * p));
       w.s_d[k] = make_float4(env_d.x, env_d.y, env_d.z, 0.f);
     }
-    k = warp_append(&w.counts[2], push_pt);
+    k = warp_append(&w.counts[kPt + qin], push_pt);
     if (push_pt) {
-      w.s_o[k] = make_float4(pt_o.x, pt_o.y, pt_o.z, __int_as_float(2 * p + 1));
-      w.s_d[k] = make_float4(pt_d.x, pt_d.y, pt_d.z, pt_dist);
-      w.s_p[k] = make_float4(pt_p.x, pt_p.y, pt_p.z, 0.f);
+      int64_t j = w.shadow_half + k;
+      w.s_o[j] = make_float4(pt_o.x, pt_o.y, pt_o.z, __int_as_float(2 * p + 1));
+      w.s_d[j] = make_float4(pt_d.x, pt_d.y, pt_d.z, pt_dist);
+      w.s_p[j] = make_float4(pt_p.x, pt_p.y, pt_p.z, 0.f);
     }
   }
 }
@@ -467,6 +495,7 @@ er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
   WaveView* w = &ww->v;
   w->aov = aov;
   w->stats = s->d_stats;
+  w->shadow_half = cap;
   er_status st;
 #define AL(ptr, bytes) \
   if ((st = alloc_w(s, ww, (void**)&(ptr), (bytes))) != ER_OK) { free_wave(s); return st; }
@@ -551,16 +580,12 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   const bool q8 = s->dev.use_q8;
   const bool count = o->flags & ER_RENDER_COUNT;
   const bool prof = o->flags & ER_RENDER_PROFILE;
-  static int g_ext[4] = {0}, g_sh[4] = {0}, g_shade = 0;
+  static int g_tr[4] = {0}, g_shade = 0;
   if (!g_shade) {
-    g_ext[0] = grid_for(k_extend<false, false>, kTravBlock, s->num_sms);
-    g_ext[1] = grid_for(k_extend<true, false>, kTravBlock, s->num_sms);
-    g_ext[2] = grid_for(k_extend<false, true>, kTravBlock, s->num_sms);
-    g_ext[3] = grid_for(k_extend<true, true>, kTravBlock, s->num_sms);
-    g_sh[0] = grid_for(k_shadow<false, false>, kTravBlock, s->num_sms);
-    g_sh[1] = grid_for(k_shadow<true, false>, kTravBlock, s->num_sms);
-    g_sh[2] = grid_for(k_shadow<false, true>, kTravBlock, s->num_sms);
-    g_sh[3] = grid_for(k_shadow<true, true>, kTravBlock, s->num_sms);
+    g_tr[0] = grid_for(k_trace<false, false>, kTravBlock, s->num_sms);
+    g_tr[1] = grid_for(k_trace<true, false>, kTravBlock, s->num_sms);
+    g_tr[2] = grid_for(k_trace<false, true>, kTravBlock, s->num_sms);
+    g_tr[3] = grid_for(k_trace<true, true>, kTravBlock, s->num_sms);
     g_shade = grid_for(k_shade, 128, s->num_sms);
   }
   const int variant = (q8 ? 1 : 0) + (count ? 2 : 0);
@@ -595,25 +620,19 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     int32_t n = cur * npix;
     k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);
     if ((st = mark(ER_STAGE_RAYGEN)) != ER_OK) return st;
-    int32_t q = 0;
-    for (int32_t b = 0; b < max_depth; b++) {
+    // trace(b): extension rays of bounce b + shadow rays of bounce b-1;
+    // the extra trace(max_depth) finishes the last bounce's shadow rays.
+    for (int32_t b = 0; b <= max_depth; b++) {
       switch (variant) {
-        case 0: k_extend<false, false><<<g_ext[0], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
-        case 1: k_extend<true, false><<<g_ext[1], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
-        case 2: k_extend<false, true><<<g_ext[2], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
-        default: k_extend<true, true><<<g_ext[3], kTravBlock, 0, s->stream>>>(s->dev, w, q, s->err_word); break;
+        case 0: k_trace<false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
+        case 1: k_trace<true, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
+        case 2: k_trace<false, true><<<g_tr[2], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
+        default: k_trace<true, true><<<g_tr[3], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
       }
-      if ((st = mark(ER_STAGE_EXTEND)) != ER_OK) return st;
-      k_shade<<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, q, b);
+      if ((st = mark(ER_STAGE_TRACE)) != ER_OK) return st;
+      if (b == max_depth) break;
+      k_shade<<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b);
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
-      switch (variant) {
-        case 0: k_shadow<false, false><<<g_sh[0], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
-        case 1: k_shadow<true, false><<<g_sh[1], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
-        case 2: k_shadow<false, true><<<g_sh[2], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
-        default: k_shadow<true, true><<<g_sh[3], kTravBlock, 0, s->stream>>>(s->dev, w, s->err_word); break;
-      }
-      if ((st = mark(ER_STAGE_SHADOW)) != ER_OK) return st;
-      q ^= 1;
     }
     if (dump_rad) {
       k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, dump_rad, dump_b);

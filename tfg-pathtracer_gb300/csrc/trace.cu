@@ -7,24 +7,28 @@ namespace er {
 namespace {
 
 template <bool Q8, bool STATS>
-__global__ void __launch_bounds__(kTravBlock)
-    k_trace_rays(DevScene S, const float* __restrict__ rays, int64_t n, int normalize, int32_t* tri, float* dist,
-                 float* uv, unsigned long long* stats, uint32_t* err) {
+__global__ void __launch_bounds__(kTravBlock, kTravMinBlocks)
+    k_trace_rays(DevScene S, const float* __restrict__ rays, int32_t n, int normalize, int32_t* tri, float* dist,
+                 float* uv, unsigned long long* stats, int32_t* counter, uint32_t* err) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
   TravStats st{0, 0, 0};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float* q = rays + 6 * i;
-    f3 o = mk(q[0], q[1], q[2]);
-    f3 d = mk(q[3], q[4], q[5]);
-    if (normalize) d = xnormalize(d);  // Ray.hpp:17
-    TravResult r = traverse<kClosest, Q8, STATS>(S, o, d, mk1(0.f), 0.f, stk + threadIdx.x, st, err);
-    tri[i] = r.slot >= 0 ? __float_as_int(__ldg(S.tri_v + 3 * (size_t)r.slot).w) : -1;
-    if (dist) dist[i] = r.slot >= 0 ? r.dist : 0.0f;
-    if (uv) {
-      uv[2 * i] = r.slot >= 0 ? r.u : 0.0f;
-      uv[2 * i + 1] = r.slot >= 0 ? r.v : 0.0f;
-    }
-  }
+  persistent_traverse<kClosest, Q8, STATS>(
+      S, n, counter, stk + threadIdx.x, st, err,
+      [&](int32_t i, auto& tr) {
+        const float* q = rays + 6 * (int64_t)i;
+        f3 o = mk(q[0], q[1], q[2]);
+        f3 d = mk(q[3], q[4], q[5]);
+        if (normalize) d = xnormalize(d);  // Ray.hpp:17
+        tr.init(S, o, d, mk1(0.f), 0.f);
+      },
+      [&](int32_t i, auto& tr) {
+        tri[i] = tr.slot >= 0 ? __float_as_int(__ldg(S.tri_v + 3 * (size_t)tr.slot).w) : -1;
+        if (dist) dist[i] = tr.slot >= 0 ? tr.best : 0.0f;
+        if (uv) {
+          uv[2 * (int64_t)i] = tr.slot >= 0 ? tr.u : 0.0f;
+          uv[2 * (int64_t)i + 1] = tr.slot >= 0 ? tr.v : 0.0f;
+        }
+      });
   if (STATS) {
     atomicAdd(&stats[8], (unsigned long long)st.nodes);
     atomicAdd(&stats[9], (unsigned long long)st.boxes);
@@ -43,8 +47,10 @@ void launch(er_scene* s, const float* rays, int64_t n, int normalize, int32_t* t
   int64_t need = (n + kTravBlock - 1) / kTravBlock;
   int g = (int)(need < grid ? need : grid);
   if (g < 1) g = 1;
-  k_trace_rays<Q8, STATS><<<g, kTravBlock, 0, s->stream>>>(s->dev, rays, n, normalize, tri, dist, uv, s->d_stats,
-                                                          s->err_word);
+  int32_t* counter = (int32_t*)((char*)s->err_word + 32);
+  cudaMemsetAsync(counter, 0, sizeof(int32_t), s->stream);
+  k_trace_rays<Q8, STATS><<<g, kTravBlock, 0, s->stream>>>(s->dev, rays, (int32_t)n, normalize, tri, dist, uv,
+                                                          s->d_stats, counter, s->err_word);
 }
 
 }  // namespace
@@ -55,6 +61,7 @@ using namespace er;
 extern "C" er_status er_trace_closest(er_scene* s, const float* rays, int64_t n, int32_t* tri_id, float* dist,
                                       float* uv, uint32_t flags, er_trace_stats* stats) {
   if (!s || n < 0 || (n > 0 && (!rays || !tri_id))) return fail(ER_ERR_INVALID_ARG, "bad argument");
+  if (n > 0x7FFFFFFF) return fail(ER_ERR_INVALID_ARG, "more than 2^31-1 rays in one call");
   ER_CUDA(cudaSetDevice(s->device));
   if (n == 0) return ER_OK;
   const bool dev = flags & ER_TRACE_DEVICE_PTRS;

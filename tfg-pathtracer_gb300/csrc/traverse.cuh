@@ -1,4 +1,4 @@
-// BVH4 traversal shared by the extension (closest-hit) and shadow kernels.
+// BVH4 traversal shared by the trace and er_trace_closest kernels.
 //
 // Reference semantics being reproduced (BVH.hpp:120-175, Tri.hpp:38-92):
 // every triangle whose Moller-Trumbore test passes is a candidate, and the
@@ -6,10 +6,16 @@
 // position is the smooth-shading position when the surface is locally convex
 // (not t).  The reference visits every leaf its (unpruned) slab test accepts;
 // ties go to the first found.  Here boxes are tested conservatively and
-// pruned with  t_near > best + delta, delta being a per-child bound on
+// pruned with  t_near - delta > limit, delta being a per-child bound on
 // |shading position - geometric hit|, so the same candidate set is ranked;
 // exact ties go to the lowest tie key (the reference's visiting order when
 // the caller supplies it, else the triangle index).
+//
+// Execution model: persistent warps, one ray per lane, lanes refilled from
+// the queue when they finish (dynamic fetch), and "while-while" scheduling:
+// a lane that reaches a leaf postpones it and keeps expanding nodes; the
+// warp intersects leaves once every lane has one (or has no node left), so
+// triangle tests run with most lanes active.
 #pragma once
 
 #include "common.cuh"
@@ -20,6 +26,10 @@ namespace er {
 enum TraceMode { kClosest = 0, kAny = 1, kPoint = 2 };
 
 constexpr int kTravBlock = 128;
+#ifndef ER_TRAV_MIN_BLOCKS
+#define ER_TRAV_MIN_BLOCKS 7
+#endif
+constexpr int kTravMinBlocks = ER_TRAV_MIN_BLOCKS;  // blocks of 128 per SM the register budget allows
 constexpr int kSmemStack = 16;
 constexpr int kLocalStack = 80;
 constexpr int kMaxStack = kSmemStack + kLocalStack;
@@ -66,48 +76,155 @@ __device__ __forceinline__ f3 ref_position(f3 o, f3 d, float t, float u, float v
   return convex ? sp : geom;
 }
 
-struct TravResult {
-  int32_t slot;  // leaf slot of the winner, -1 = miss
-  float t, u, v, dist;
-  f3 pos;
-  bool occluded;
-};
-
 __device__ __forceinline__ float byte_of(uint32_t w, int c) { return (float)((w >> (8 * c)) & 0xFFu); }
 
-// One traversal.  MODE kClosest: closest hit by reference distance.
-// kAny: any triangle hit (env shadow rays, kernel.cu:247-248).  kPoint:
-// point-light shadow ray: occluded when the closest hit (by distance from
-// the shadow origin o) lies closer than pdist to the shading point pp
-// (kernel.cu:192-197); the search stops early once a hit proves it.
+// Three-input min / max (PTX ISA 8.8, sm_100+); a NaN input is ignored.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// MODE kClosest: closest hit by reference distance.  kAny: any triangle hit
+// (env shadow rays, kernel.cu:247-248).  kPoint: point-light shadow ray:
+// occluded when the closest hit (by distance from the shadow origin o) lies
+// closer than pdist to the shading point pp (kernel.cu:192-197).  Only hits
+// whose reference distance is below Tp = pdist + |o - pp| can occlude, and
+// when one exists the closest hit is among them, so the search is pruned at
+// Tp and stops at the first hit that already proves occlusion.
+//
+// Stack entries are (node or leaf reference, lower bound of the reference
+// distance of anything below it); leaves and internal nodes share the stack.
 template <int MODE, bool Q8, bool STATS>
-__device__ __forceinline__ TravResult traverse(const DevScene& S, f3 o, f3 d, f3 pp, float pdist, int2* sstk,
-                                               TravStats& st, uint32_t* err) {
-  int2 lstk[kLocalStack];
-  TravResult R;
-  R.slot = -1;
-  R.t = R.u = R.v = 0.0f;
-  R.dist = INFINITY;
-  R.pos = mk1(0.0f);
-  R.occluded = false;
-  uint32_t bkey = 0xFFFFFFFFu;
-  const f3 inv = mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
-  const float omax = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
-  const float slack = (omax + S.scene_eps) * 2.0e-6f;
-  // point mode: |o - pp| bounds how far the distances from o and pp differ
-  const float poff = (MODE == kPoint) ? xlen(xsub(o, pp)) * 1.000001f + slack : 0.0f;
-  int sp = 0;
-  int32_t node = 0;
-  bool done = false;
-  // A ray visits every node at most once; a longer walk means a corrupt
-  // tree, reported through the error word instead of spinning.
-  int64_t guard = S.n_nodes + 1;
-  while (!done) {
+struct Traverser {
+  f3 o, d, inv, pp;
+  // Slab planes are evaluated as fma(plane, inv, bias): the near-plane bias
+  // is lowered and the far-plane bias raised by a bound on the rounding
+  // error, so a box the exact ray touches is never culled.
+  f3 bnear, bfar;
+  uint32_t sgn;  // bit a set: direction component a is negative
+  float slack, poff, pdist, tp;
+  float best;       // reference distance of the current winner
+  uint32_t bkey;
+  int32_t slot;     // leaf slot of the winner, -1 = none
+  float t, u, v;
+  f3 pos;
+  bool occluded;
+  bool done;
+  int sp;
+  int32_t node;     // next internal node to expand, -1 = none
+  int32_t leaf;     // postponed leaf reference, 0 = none
+  float leaf_key;
+  int32_t guard;
+
+  __device__ __forceinline__ float limit() const {
+    return MODE == kPoint ? fminf(best, tp) : best;
+  }
+  __device__ __forceinline__ bool survives(float key) const {
+    return MODE == kAny || key <= limit() * 1.000001f + slack;
+  }
+
+  __device__ __forceinline__ void init(const DevScene& S, f3 o_, f3 d_, f3 pp_, float pdist_) {
+    o = o_;
+    d = d_;
+    pp = pp_;
+    pdist = pdist_;
+    // A zero direction component gets a huge finite reciprocal (2^100) so
+    // that fma(plane, inv, -o*inv) still separates planes on either side of
+    // the origin instead of producing inf - inf.
+    const float big = 1.26765060e30f;  // 2^100
+    inv = mk(d.x != 0.0f ? __frcp_rn(d.x) : copysignf(big, d.x), d.y != 0.0f ? __frcp_rn(d.y) : copysignf(big, d.y),
+             d.z != 0.0f ? __frcp_rn(d.z) : copysignf(big, d.z));
+    float omax = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    slack = (omax + S.scene_eps) * 2.0e-6f;
+    // |error| of fma(plane, inv, -o*inv) <= (|o| + |plane|) |inv| 2^-23;
+    // node planes lie within +-scene_eps.  Margin: 4x that.  It only widens
+    // slabs whose plane lies within ~1e-5 (|o| + scene_eps) of the origin.
+    const float k = 4.76837158e-7f;  // 2^-21
+    float mx = (fabsf(o.x) + S.scene_eps) * fabsf(inv.x) * k;
+    float my = (fabsf(o.y) + S.scene_eps) * fabsf(inv.y) * k;
+    float mz = (fabsf(o.z) + S.scene_eps) * fabsf(inv.z) * k;
+    f3 oi = mk(-(o.x * inv.x), -(o.y * inv.y), -(o.z * inv.z));
+    bnear = mk(oi.x - mx, oi.y - my, oi.z - mz);
+    bfar = mk(oi.x + mx, oi.y + my, oi.z + mz);
+    sgn = (__float_as_uint(inv.x) >> 31) | ((__float_as_uint(inv.y) >> 31) << 1) |
+          ((__float_as_uint(inv.z) >> 31) << 2);
+    poff = (MODE == kPoint) ? xlen(xsub(o, pp)) * 1.000001f + slack : 0.0f;
+    tp = (MODE == kPoint) ? (pdist + poff) * 1.000001f + slack : INFINITY;
+    best = INFINITY;
+    bkey = 0xFFFFFFFFu;
+    slot = -1;
+    t = u = v = 0.0f;
+    pos = mk1(0.0f);
+    occluded = false;
+    done = false;
+    sp = 0;
+    node = 0;
+    leaf = 0;
+    leaf_key = 0.0f;
+    // a ray visits every node at most once; a longer walk means a corrupt tree
+    guard = (int32_t)min(S.n_nodes + 1, (int64_t)0x7FFFFFFF);
+  }
+
+  __device__ __forceinline__ bool push(int2* sstk, int2* lstk, int32_t ref, float key, uint32_t* err) {
+    if (sp >= kMaxStack) {
+      atomicOr(err, 1u);
+      done = true;
+      return false;
+    }
+    int2 e = make_int2(ref, __float_as_int(key));
+    if (sp < kSmemStack) sstk[sp * kTravBlock] = e;
+    else lstk[sp - kSmemStack] = e;
+    sp++;
+    return true;
+  }
+
+  __device__ __forceinline__ void finish() {
+    done = true;
+    if (MODE == kPoint && slot >= 0) occluded = xlen(xsub(pos, pp)) < pdist;  // kernel.cu:194-196
+  }
+
+  // Pops entries until an internal node survives the bound (-> node) or the
+  // stack is empty.  A surviving leaf is taken as the postponed leaf when
+  // the slot is free; with the slot taken it is pushed back and the lane
+  // waits for the next leaf round.
+  __device__ __forceinline__ void pop_next(int2* sstk, int2* lstk, uint32_t* err) {
+    node = -1;
+    while (sp > 0) {
+      int2 e = (sp - 1) < kSmemStack ? sstk[(sp - 1) * kTravBlock] : lstk[sp - 1 - kSmemStack];
+      float key = __int_as_float(e.y);
+      if (!survives(key)) {
+        sp--;
+        continue;
+      }
+      if (e.x >= 0) {
+        sp--;
+        node = e.x;
+        return;
+      }
+      if (leaf != 0) return;  // keep it on the stack
+      sp--;
+      leaf = e.x;
+      leaf_key = key;
+    }
+    if (leaf == 0) finish();
+  }
+
+  // Expands `node`: tests its four child boxes, postpones / pushes leaf
+  // children, pushes the farther internal children and continues with the
+  // nearest.
+  __device__ __forceinline__ void node_step(const DevScene& S, int2* sstk, int2* lstk, TravStats& st, uint32_t* err) {
     if (--guard < 0 || (uint64_t)node >= (uint64_t)S.n_nodes) {
       atomicOr(err, 4u);
-      return R;
+      done = true;
+      return;
     }
-    float4 lx, hx, ly, hy, lz, hz, dl;
+    float4 nx, fx, ny, fy, nz, fz, dl;
     int4 ch;
     if (Q8) {
       const uint4* qn = S.qnodes + 4 * (size_t)node;
@@ -115,85 +232,58 @@ __device__ __forceinline__ TravResult traverse(const DevScene& S, f3 o, f3 d, f3
       float ox = __uint_as_float(a.x), oy = __uint_as_float(a.y), oz = __uint_as_float(a.z);
       float sx = __uint_as_float((a.w & 0xFFu) << 23), sy = __uint_as_float(((a.w >> 8) & 0xFFu) << 23),
             sz = __uint_as_float(((a.w >> 16) & 0xFFu) << 23);
-      lx = make_float4(ox + byte_of(b.x, 0) * sx, ox + byte_of(b.x, 1) * sx, ox + byte_of(b.x, 2) * sx, ox + byte_of(b.x, 3) * sx);
-      hx = make_float4(ox + byte_of(b.y, 0) * sx, ox + byte_of(b.y, 1) * sx, ox + byte_of(b.y, 2) * sx, ox + byte_of(b.y, 3) * sx);
-      ly = make_float4(oy + byte_of(b.z, 0) * sy, oy + byte_of(b.z, 1) * sy, oy + byte_of(b.z, 2) * sy, oy + byte_of(b.z, 3) * sy);
-      hy = make_float4(oy + byte_of(b.w, 0) * sy, oy + byte_of(b.w, 1) * sy, oy + byte_of(b.w, 2) * sy, oy + byte_of(b.w, 3) * sy);
-      lz = make_float4(oz + byte_of(c.x, 0) * sz, oz + byte_of(c.x, 1) * sz, oz + byte_of(c.x, 2) * sz, oz + byte_of(c.x, 3) * sz);
-      hz = make_float4(oz + byte_of(c.y, 0) * sz, oz + byte_of(c.y, 1) * sz, oz + byte_of(c.y, 2) * sz, oz + byte_of(c.y, 3) * sz);
+      uint32_t qnx = (sgn & 1u) ? b.y : b.x, qfx = (sgn & 1u) ? b.x : b.y;
+      uint32_t qny = (sgn & 2u) ? b.w : b.z, qfy = (sgn & 2u) ? b.z : b.w;
+      uint32_t qnz = (sgn & 4u) ? c.y : c.x, qfz = (sgn & 4u) ? c.x : c.y;
+      nx = make_float4(ox + byte_of(qnx, 0) * sx, ox + byte_of(qnx, 1) * sx, ox + byte_of(qnx, 2) * sx, ox + byte_of(qnx, 3) * sx);
+      fx = make_float4(ox + byte_of(qfx, 0) * sx, ox + byte_of(qfx, 1) * sx, ox + byte_of(qfx, 2) * sx, ox + byte_of(qfx, 3) * sx);
+      ny = make_float4(oy + byte_of(qny, 0) * sy, oy + byte_of(qny, 1) * sy, oy + byte_of(qny, 2) * sy, oy + byte_of(qny, 3) * sy);
+      fy = make_float4(oy + byte_of(qfy, 0) * sy, oy + byte_of(qfy, 1) * sy, oy + byte_of(qfy, 2) * sy, oy + byte_of(qfy, 3) * sy);
+      nz = make_float4(oz + byte_of(qnz, 0) * sz, oz + byte_of(qnz, 1) * sz, oz + byte_of(qnz, 2) * sz, oz + byte_of(qnz, 3) * sz);
+      fz = make_float4(oz + byte_of(qfz, 0) * sz, oz + byte_of(qfz, 1) * sz, oz + byte_of(qfz, 2) * sz, oz + byte_of(qfz, 3) * sz);
       ch = make_int4((int)c.z, (int)c.w, (int)e.x, (int)e.y);
       float dd = __uint_as_float(e.z);
       dl = make_float4(dd, dd, dd, dd);
     } else {
       const float4* nd = S.nodes + 8 * (size_t)node;
-      lx = __ldg(nd + 0); hx = __ldg(nd + 1); ly = __ldg(nd + 2); hy = __ldg(nd + 3);
-      lz = __ldg(nd + 4); hz = __ldg(nd + 5);
+      nx = __ldg(nd + (sgn & 1u)); fx = __ldg(nd + 1 - (sgn & 1u));
+      ny = __ldg(nd + 2 + ((sgn >> 1) & 1u)); fy = __ldg(nd + 3 - ((sgn >> 1) & 1u));
+      nz = __ldg(nd + 4 + ((sgn >> 2) & 1u)); fz = __ldg(nd + 5 - ((sgn >> 2) & 1u));
       float4 c4 = __ldg(nd + 6);
       ch = make_int4(__float_as_int(c4.x), __float_as_int(c4.y), __float_as_int(c4.z), __float_as_int(c4.w));
       dl = __ldg(nd + 7);
     }
     if (STATS) { st.nodes++; st.boxes += 4; }
-    float tn[4];
-    int32_t cc[4];
-    const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-    const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-    const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+    const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
+    const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
+    const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
     const float dla[4] = {dl.x, dl.y, dl.z, dl.w};
     const int32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
+    const float lim = limit() * 1.000001f + slack;
+    float ik[4];
+    int32_t ic[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      float t0x = (lxa[c] - o.x) * inv.x, t1x = (hxa[c] - o.x) * inv.x;
-      float t0y = (lya[c] - o.y) * inv.y, t1y = (hya[c] - o.y) * inv.y;
-      float t0z = (lza[c] - o.z) * inv.z, t1z = (hza[c] - o.z) * inv.z;
-      float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-      float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-      tfar = tfar + fabsf(tfar) * 1.0e-6f + slack;
-      bool hit = cha[c] != kEmpty && tnear <= tfar && tfar >= 0.0f;
-      if (MODE != kAny) hit = hit && (tnear - dla[c]) <= R.dist * 1.000001f + slack;
-      tn[c] = hit ? tnear - (MODE != kAny ? dla[c] : 0.0f) : INFINITY;
-      cc[c] = hit ? cha[c] : kEmpty;
-    }
-    // leaves first
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      if (cc[c] == kEmpty || cc[c] >= 0) continue;
-      if (!(tn[c] <= R.dist * 1.000001f + slack)) continue;  // best may have improved
-      uint32_t lf = (uint32_t)cc[c];
-      uint32_t first = lf & kLeafFirstMask, cnt = ((lf >> kLeafCountShift) & 0xFu) + 1u;
-      for (uint32_t k = 0; k < cnt; k++) {
-        uint32_t slot = first + k;
-        const float4* tv = S.tri_v + 3 * (size_t)slot;
-        float4 a = __ldg(tv), b = __ldg(tv + 1), e = __ldg(tv + 2);
-        if (STATS) st.tris++;
-        float t, u, v;
-        f3 v0 = from4(a), v1 = from4(b), v2 = from4(e);
-        if (!mt_hit(v0, v1, v2, o, d, t, u, v)) continue;
-        if (MODE == kAny) {
-          R.occluded = true;
-          R.slot = (int32_t)slot;
-          return R;
-        }
-        const float4* tnp = S.tri_n + 3 * (size_t)slot;
-        f3 pos = ref_position(o, d, t, u, v, v0, v1, v2, from4(__ldg(tnp)), from4(__ldg(tnp + 1)),
-                              from4(__ldg(tnp + 2)), nullptr);
-        float dist = xlen(xsub(pos, o));
-        uint32_t key = __float_as_uint(b.w);
-        if (dist < R.dist || (dist == R.dist && key < bkey)) {
-          R.dist = dist; R.slot = (int32_t)slot; R.t = t; R.u = u; R.v = v; R.pos = pos; bkey = key;
-          if (MODE == kPoint && (dist + poff) * 1.000001f < pdist) {
-            R.occluded = true;
-            return R;
-          }
+      float tnear = max3f(fmaf(nxa[c], inv.x, bnear.x), fmaf(nya[c], inv.y, bnear.y), fmaf(nza[c], inv.z, bnear.z));
+      float tfar = min3f(fmaf(fxa[c], inv.x, bfar.x), fmaf(fya[c], inv.y, bfar.y), fmaf(fza[c], inv.z, bfar.z));
+      bool hit = cha[c] != kEmpty && tnear <= tfar && tfar >= -slack;
+      float key = MODE == kAny ? tnear : tnear - dla[c];
+      if (MODE != kAny) hit = hit && key <= lim;
+      bool is_leaf = cha[c] < 0;
+      if (hit && is_leaf) {
+        if (leaf == 0) {
+          leaf = cha[c];
+          leaf_key = key;
+        } else if (!push(sstk, lstk, cha[c], key, err)) {
+          return;
         }
       }
-      cc[c] = kEmpty;
+      ik[c] = hit && !is_leaf ? key : INFINITY;
+      ic[c] = cha[c];
     }
     // internal children: nearest first
-    float k0 = cc[0] >= 0 && cc[0] != kEmpty ? tn[0] : INFINITY;
-    float k1 = cc[1] >= 0 && cc[1] != kEmpty ? tn[1] : INFINITY;
-    float k2 = cc[2] >= 0 && cc[2] != kEmpty ? tn[2] : INFINITY;
-    float k3 = cc[3] >= 0 && cc[3] != kEmpty ? tn[3] : INFINITY;
-    int32_t c0 = cc[0], c1 = cc[1], c2 = cc[2], c3 = cc[3];
+    float k0 = ik[0], k1 = ik[1], k2 = ik[2], k3 = ik[3];
+    int32_t c0 = ic[0], c1 = ic[1], c2 = ic[2], c3 = ic[3];
 #define ER_CSWAP(ka, ca, kb, cb)                         \
   if (kb < ka) {                                         \
     float tk = ka; ka = kb; kb = tk;                     \
@@ -205,36 +295,114 @@ __device__ __forceinline__ TravResult traverse(const DevScene& S, f3 o, f3 d, f3
     ER_CSWAP(k1, c1, k3, c3);
     ER_CSWAP(k1, c1, k2, c2);
 #undef ER_CSWAP
-    int n = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
-    if (n > 0) {
-      // push the farther ones, farthest first
-      if (sp + n - 1 > kMaxStack) {
-        atomicOr(err, 1u);
-        return R;
-      }
-      if (n > 3) { int2 e = make_int2(c3, __float_as_int(k3)); if (sp < kSmemStack) sstk[sp * kTravBlock] = e; else lstk[sp - kSmemStack] = e; sp++; }
-      if (n > 2) { int2 e = make_int2(c2, __float_as_int(k2)); if (sp < kSmemStack) sstk[sp * kTravBlock] = e; else lstk[sp - kSmemStack] = e; sp++; }
-      if (n > 1) { int2 e = make_int2(c1, __float_as_int(k1)); if (sp < kSmemStack) sstk[sp * kTravBlock] = e; else lstk[sp - kSmemStack] = e; sp++; }
+    if (k3 < INFINITY && !push(sstk, lstk, c3, k3, err)) return;
+    if (k2 < INFINITY && !push(sstk, lstk, c2, k2, err)) return;
+    if (k1 < INFINITY && !push(sstk, lstk, c1, k1, err)) return;
+    if (k0 < INFINITY) {
       node = c0;
-      continue;
+      return;
     }
-    // pop until an entry survives the (possibly tightened) bound
-    done = true;
-    while (sp > 0) {
-      sp--;
-      int2 e = sp < kSmemStack ? sstk[sp * kTravBlock] : lstk[sp - kSmemStack];
-      if (MODE == kAny || __int_as_float(e.y) <= R.dist * 1.000001f + slack) {
-        node = e.x;
-        done = false;
-        break;
+    pop_next(sstk, lstk, err);
+  }
+
+  // Intersects the triangles of the postponed leaf, then pops on if the lane
+  // has no node left.
+  __device__ __forceinline__ void leaf_step(const DevScene& S, int2* sstk, int2* lstk, TravStats& st, uint32_t* err) {
+    uint32_t lf = (uint32_t)leaf;
+    leaf = 0;
+    if (survives(leaf_key)) {
+      uint32_t first = lf & kLeafFirstMask, cnt = ((lf >> kLeafCountShift) & 0xFu) + 1u;
+      for (uint32_t k = 0; k < cnt; k++) {
+        uint32_t sl = first + k;
+        const float4* tv = S.tri_v + 3 * (size_t)sl;
+        float4 a = __ldg(tv), b = __ldg(tv + 1), e = __ldg(tv + 2);
+        if (STATS) st.tris++;
+        float tt, uu, vv;
+        f3 v0 = from4(a), v1 = from4(b), v2 = from4(e);
+        if (!mt_hit(v0, v1, v2, o, d, tt, uu, vv)) continue;
+        if (MODE == kAny) {
+          occluded = true;
+          slot = (int32_t)sl;
+          done = true;
+          return;
+        }
+        const float4* tnp = S.tri_n + 3 * (size_t)sl;
+        f3 p = ref_position(o, d, tt, uu, vv, v0, v1, v2, from4(__ldg(tnp)), from4(__ldg(tnp + 1)),
+                            from4(__ldg(tnp + 2)), nullptr);
+        float dist = xlen(xsub(p, o));
+        uint32_t key = __float_as_uint(b.w);
+        if (dist < best || (dist == best && key < bkey)) {
+          best = dist; slot = (int32_t)sl; t = tt; u = uu; v = vv; pos = p; bkey = key;
+          if (MODE == kPoint && (dist + poff) * 1.000001f < pdist) {
+            occluded = true;  // the closest hit is at least this close
+            done = true;
+            return;
+          }
+        }
       }
     }
+    if (node < 0) pop_next(sstk, lstk, err);
   }
-  if (MODE == kPoint && R.slot >= 0) {
-    // kernel.cu:194-196 on the closest hit: |hit - point| < dist
-    R.occluded = xlen(xsub(R.pos, pp)) < pdist;
+};
+
+#ifndef ER_REFILL_THRESHOLD
+#define ER_REFILL_THRESHOLD 20
+#endif
+// Lanes below this many active rays make the warp refill from the queue.
+constexpr int kRefillThreshold = ER_REFILL_THRESHOLD;
+
+// Persistent, warp-refilling traversal over a queue of n items.  `load(i,
+// tr)` initialises lane state for item i, `store(i, tr)` consumes a finished
+// traversal.  Items are claimed in warp batches from *counter, which must be
+// zero at launch.
+template <int MODE, bool Q8, bool STATS, typename Load, typename Store>
+__device__ __forceinline__ void persistent_traverse(const DevScene& S, int32_t n, int32_t* counter, int2* sstk,
+                                                    TravStats& st, uint32_t* err, Load load, Store store) {
+  int2 lstk[kLocalStack];
+  Traverser<MODE, Q8, STATS> tr;
+  const unsigned lane = threadIdx.x & 31u;
+  int32_t item = -1;  // -1: needs an item; >= n: queue exhausted
+  bool active = false;
+  while (true) {
+    bool need = item < 0;
+    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    if (m) {
+      int leader = __ffs(m) - 1;
+      int32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(counter, __popc(m));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        item = base + __popc(m & ((1u << lane) - 1u));
+        if (item >= n) item = n;  // exhausted
+        else {
+          load(item, tr);
+          active = true;
+        }
+      }
+    }
+    if (!__any_sync(0xFFFFFFFFu, active)) break;
+    while (true) {
+      // leaf round once no active lane is left with only node work
+      bool node_only = active && tr.node >= 0 && tr.leaf == 0;
+      bool leaf_round = !__any_sync(0xFFFFFFFFu, node_only);
+      if (active) {
+        if (leaf_round) {
+          if (tr.leaf != 0) tr.leaf_step(S, sstk, lstk, st, err);
+        } else if (tr.node >= 0) {
+          tr.node_step(S, sstk, lstk, st, err);
+        }
+        if (tr.done) {
+          store(item, tr);
+          active = false;
+          item = -1;
+        }
+      }
+      unsigned am = __ballot_sync(0xFFFFFFFFu, active);
+      unsigned want = __ballot_sync(0xFFFFFFFFu, item < 0);
+      if (__popc(am) < kRefillThreshold && want) break;
+      if (!am) break;
+    }
   }
-  return R;
 }
 
 }  // namespace er

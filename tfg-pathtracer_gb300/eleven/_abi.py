@@ -123,7 +123,7 @@ class er_render_opts(C.Structure):
 
 ER_RENDER_PROFILE = 1 << 6
 ER_RENDER_COUNT = 1 << 7
-STAGES = ["raygen", "extend", "shade", "shadow", "accumulate"]
+STAGES = ["raygen", "trace", "shade", "reserved", "accumulate"]
 
 
 class er_render_stats(C.Structure):

@@ -28,6 +28,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
+# extra nvcc flags (tuning sweeps); a change needs build_product(force=True)
+CU_FLAGS += os.environ.get("ELEVEN_NVCC_FLAGS", "").split()
 
 SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp",
            "trace.cu", "render.cu"]
