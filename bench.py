@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch-rays", type=int, default=-1,
+                    help="print the rays traced by trace launch B of a 1-spp wave (extension rays of bounce B "
+                         "+ shadow rays of bounce B-1) and exit; used to turn an ncu capture of that launch "
+                         "into DRAM bytes per ray")
     return ap.parse_args()
 
 
@@ -320,8 +324,36 @@ def run_gpu(args):
     return 0
 
 
+def launch_rays(args):
+    """Rays in trace launch b of a 1-spp wave at sample index 1 (the first
+    warm-up step of the default run): extension rays of bounce b plus shadow
+    rays of bounce b-1, from the ray counters of depth-limited renders."""
+    from eleven import _abi as A
+    from eleven import _lib
+    arrays, max_depth, cfg = make_scene(args.config)
+    scene = _lib.Scene(arrays)
+    b = args.launch_rays
+
+    def counts(depth):
+        if depth == 0:
+            return 0, 0
+        st = scene.render(spp=1, max_depth=depth, sample_begin=1, flags=A.ER_RENDER_NO_OUTPUT)["stats"]
+        return st.rays_closest, st.rays_shadow
+
+    c_b1, _ = counts(b + 1)
+    c_b, s_b = counts(b)
+    _, s_bm1 = counts(b - 1) if b >= 1 else (0, 0)
+    ext = c_b1 - c_b
+    shadow = s_b - s_bm1
+    print(json.dumps({"launch": b, "extension_rays": int(ext), "shadow_rays": int(shadow),
+                      "rays": int(ext + shadow), "config": args.config}))
+    return 0
+
+
 def main():
     args = parse()
+    if args.launch_rays >= 0:
+        return launch_rays(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -160,6 +160,9 @@ er_status er_scene_load(const char* dir, const er_scene_opts* opts,
 er_status er_scene_info_get(const er_scene* scene, er_scene_info* out);
 /* Replace the camera of a built scene (no BVH rebuild). */
 er_status er_scene_set_camera(er_scene* scene, const er_camera* cam);
+/* Current camera of a scene (resolution of the film; the camera a loaded
+ * scene.json describes, SceneLoader.hpp:25-46). */
+er_status er_scene_get_camera(const er_scene* scene, er_camera* out);
 er_status er_scene_free(er_scene* scene);
 
 /* ---------------------------------------------------------------- render -- */

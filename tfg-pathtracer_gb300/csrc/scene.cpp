@@ -362,6 +362,12 @@ extern "C" er_status er_scene_set_camera(er_scene* s, const er_camera* c) {
   return ER_OK;
 }
 
+extern "C" er_status er_scene_get_camera(const er_scene* s, er_camera* out) {
+  if (!s || !out) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+  *out = s->camera;
+  return ER_OK;
+}
+
 extern "C" er_status er_scene_free(er_scene* s) {
   if (!s) return ER_OK;
   cudaSetDevice(s->device);

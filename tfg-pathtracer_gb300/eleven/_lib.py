@@ -51,6 +51,8 @@ def load(build_if_missing=True):
     L.er_scene_info_get.argtypes = [C.c_void_p, C.POINTER(A.er_scene_info)]
     L.er_scene_set_camera.restype = A.er_status
     L.er_scene_set_camera.argtypes = [C.c_void_p, C.POINTER(A.er_camera)]
+    L.er_scene_get_camera.restype = A.er_status
+    L.er_scene_get_camera.argtypes = [C.c_void_p, C.POINTER(A.er_camera)]
     L.er_scene_free.restype = A.er_status
     L.er_scene_free.argtypes = [C.c_void_p]
     L.er_render.restype = A.er_status
@@ -128,8 +130,16 @@ class Scene:
 
     @property
     def resolution(self):
-        cam = self.arrays.camera
-        return int(cam["x_res"]), int(cam["y_res"])
+        c = self.camera()
+        return int(c.x_res), int(c.y_res)
+
+    def camera(self):
+        c = A.er_camera()
+        check(load().er_scene_get_camera(self.h, C.byref(c)), "er_scene_get_camera")
+        return c
+
+    def set_camera(self, cam):
+        check(load().er_scene_set_camera(self.h, C.byref(cam)), "er_scene_set_camera")
 
     def trace(self, rays, normalize=True, stats=False):
         rays = np.ascontiguousarray(rays, dtype=np.float32)

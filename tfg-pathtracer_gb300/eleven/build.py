@@ -20,6 +20,7 @@ ROOT = os.path.dirname(PKG_ROOT)                     # repository root
 CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(PKG_ROOT, "libeleven.so")
+CLI = os.path.join(PKG_ROOT, "bin", "eleven")  # the command-line renderer
 INCLUDE = os.path.join(ROOT, "include")
 ORACLE = os.path.join(ROOT, "oracle")
 REF_SRC = os.environ.get("ELEVEN_REF_DIR", "/root/reference/src/tfg-pathtracer")
@@ -78,6 +79,11 @@ def build_product(force=False, verbose=False):
                 sys.stdout.write(o)
     if force or jobs or _stale(LIB, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"])
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    if force or _stale(CLI, [cli_src, LIB, os.path.join(INCLUDE, "eleven.h")]):
+        os.makedirs(os.path.dirname(CLI), exist_ok=True)
+        _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", CLI, "-L" + PKG_ROOT, "-leleven",
+              "-Wl,-rpath,$ORIGIN/.."])
     return LIB
 
 

@@ -85,6 +85,7 @@ class SceneArrays:
     tangents: np.ndarray = None
     tangent_sign: np.ndarray = None
     tie_key: np.ndarray = None
+    texture_bytes: list = None     # 8-bit sources of `textures`, rows bottom-first
     name: str = "scene"
 
     @property
@@ -318,6 +319,41 @@ def sphere_uv(verts):
     return np.stack([u, v], -1)
 
 
+def ref_normalize(n):
+    """Vector3::normalized in float32 (Vector.hpp:173-176), iterated to a
+    fixed point so that a loader that normalises normals again
+    (ObjLoader.hpp:118) reproduces them bit for bit."""
+    def once(v):
+        x, y, z = v[:, 0], v[:, 1], v[:, 2]
+        ln = np.sqrt(x * x + y * y + z * z)
+        nz = ln != 0
+        m = v.copy()
+        m[nz] = v[nz] / ln[nz, None]
+        return m
+
+    def fixed(v):
+        return (once(v).view(np.uint32) == v.view(np.uint32)).all(1)
+
+    n = once(np.asarray(n, np.float32).reshape(-1, 3).copy())
+    bad = np.nonzero(~fixed(n))[0]
+    if len(bad):
+        # some vectors alternate between two roundings: search the 1-ulp
+        # neighbourhood for a fixed point
+        steps = np.array([(a, b, c) for a in (0, -1, 1) for b in (0, -1, 1) for c in (0, -1, 1)], np.int64)
+        v = n[bad]
+        bits = v.view(np.int32).astype(np.int64)
+        for s in steps[1:]:
+            cand = (bits + s[None, :]).astype(np.int32).view(np.float32)
+            ok = fixed(cand)
+            v[ok] = cand[ok]
+            bits[ok] = v[ok].view(np.int32)
+            still = ~fixed(v)
+            if not still.any():
+                break
+        n[bad] = v
+    return n
+
+
 def _assemble(meshes):
     """meshes: list of (verts(V,3), faces(F,3), normals(V,3), uv(V,2))."""
     P, N, U, O = [], [], [], []
@@ -326,8 +362,8 @@ def _assemble(meshes):
         N.append(n[f])
         U.append(uv[f])
         O.append(np.full(len(f), oi, np.int32))
-    return (np.concatenate(P).astype(np.float32), np.concatenate(N).astype(np.float32),
-            np.concatenate(U).astype(np.float32), np.concatenate(O))
+    N = ref_normalize(np.concatenate(N)).reshape(-1, 3, 3)
+    return (np.concatenate(P).astype(np.float32), N, np.concatenate(U).astype(np.float32), np.concatenate(O))
 
 
 def ground_quad(y, half):
@@ -419,7 +455,7 @@ def config1(x_res=1920, y_res=1080, seed=1, n_meshes=200, tri_lo=1000, tri_hi=20
                          roughness=rng.uniform(0.05, 1.0), metallic=float(rng.uniform() < 0.3),
                          specular=0.5, clearcoat=rng.uniform(0, 1), sheen=rng.uniform(0, 1)))
     P, N, U, O = _assemble(meshes)
-    texs, _ = noise_textures(n_tex, tex_size, seed)
+    texs, tex_bytes = noise_textures(n_tex, tex_size, seed)
     focal = pinhole_focal(50.0)
     cam = dict(x_res=x_res, y_res=y_res, focal_length=focal, position=(0.0, 0.5, -16.0),
                rotation=(0.0, 0.0, 0.0), bokeh=True,
@@ -428,7 +464,8 @@ def config1(x_res=1920, y_res=1080, seed=1, n_meshes=200, tri_lo=1000, tri_hi=20
                        [[0, 10, 6], [80, 80, 80]], [[0, -2, -10], [30, 30, 40]]], np.float32)
     return SceneArrays(camera=cam, positions=P, normals=N, uvs=U, tri_object=O,
                        object_material=np.arange(len(meshes), dtype=np.int32), materials=mats,
-                       textures=texs, lights=lights, env=lognormal_env(env_w, env_h, seed), name="c1")
+                       textures=texs, texture_bytes=tex_bytes, lights=lights,
+                       env=lognormal_env(env_w, env_h, seed), name="c1")
 
 
 def random_rays(scene, n, seed=3):
