@@ -228,6 +228,30 @@ er_status er_film_read(er_scene* scene, uint32_t flags, float* beauty,
                        float* normal, float* tangent, float* bitangent,
                        uint32_t* samples, uint32_t* pathcount);
 
+/* Allocation-free render.  No counterpart in the reference: it is for
+ * callers that may not allocate device memory while rendering (a host
+ * application with a device-memory budget fixed at start-up, a render thread
+ * that may not enter the CUDA allocator).  The call allocates nothing: the
+ * path state and ray queues live in one file-scope device array sized for
+ * ER_NOALLOC_MAX_PATHS paths (about 19 MB, held on every GPU that loads the
+ * library until the process exits), and the film is the caller's device
+ * buffers: beauty W*H*4 floats (16-byte aligned), samples and pathcount
+ * W*H uint32, laid out as in er_render.
+ *  - W*H must not exceed ER_NOALLOC_MAX_PATHS (ER_ERR_INVALID_ARG otherwise);
+ *    spp is traced in waves of floor(ER_NOALLOC_MAX_PATHS / (W*H)) samples.
+ *  - Only ER_RENDER_CONTINUE is accepted in opts->flags (FP32 running mean,
+ *    no AOVs); without it the film is cleared first.
+ *  - The first call on a device looks up the array's device address (with
+ *    that device current); make that first call before any stream capture.
+ *  - All calls share the array and it keeps the last call's contents (each
+ *    wave re-initialises what it reads).  Calls whose work overlaps on the
+ *    GPU (other streams, other threads) race on it: serialise them.
+ * Synchronous like er_render.  Results equal er_render's for the same
+ * options. */
+#define ER_NOALLOC_MAX_PATHS 65536
+er_status er_render_noalloc(er_scene* scene, const er_render_opts* opts, float* beauty, uint32_t* samples,
+                            uint32_t* pathcount);
+
 /* Per-path debug output of one wave: radiance (before the clamp of
  * kernel.cu:447) and bounce count of path (pixel p, sample s) for
  * s in [sample_begin, sample_begin+spp).  radiance is spp*W*H*3 floats,

@@ -12,6 +12,8 @@
 // not depend on queue order.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "internal.h"
 #include "shade.cuh"
@@ -772,4 +774,152 @@ extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float
   cudaFree(d_b);
   if (st == ER_OK) st = check_device_error(s);
   return st;
+}
+
+// ------------------------------------------------------------------------
+// Allocation-free rendering (er_render_noalloc).
+//
+// Some callers must not allocate device memory while they render: a host
+// application that sizes its whole GPU budget once at start-up and forbids
+// allocations afterwards (an editor's live preview pane next to its own
+// renderer, a service with a fixed per-tenant memory quota), or a caller
+// whose render thread may not enter the CUDA allocator at all.  For them the
+// wavefront's scratch (path state and ray queues) lives in one file-scope
+// __device__ array sized for ER_NOALLOC_MAX_PATHS paths per wave; the film is
+// the caller's own device buffers.  The array exists on every GPU that loads
+// this library, for the life of the process.
+
+namespace er {
+namespace {
+
+constexpr int64_t kNoAllocPaths = ER_NOALLOC_MAX_PATHS;
+constexpr size_t pad256(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t kNoAllocBytes = 2 * pad256(kNoAllocPaths * 16)      // throughput, radiance
+                                 + pad256(kNoAllocPaths * 64)        // pending MIS terms
+                                 + pad256(kNoAllocPaths * 2)         // visibility
+                                 + pad256(kNoAllocPaths * 4)         // bounce counts
+                                 + 4 * pad256(kNoAllocPaths * 16)    // two extension queues
+                                 + pad256(kNoAllocPaths * 16)        // hits
+                                 + 3 * pad256(kNoAllocPaths * 32)    // shadow queue (two halves)
+                                 + pad256(16 * 4) + pad256(16 * 8);  // queue counters, ray counters
+
+}  // namespace
+}  // namespace er
+
+// The scratch of er_render_noalloc (about 19 MB for 65,536 paths).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[er::kNoAllocBytes];
+
+namespace er {
+namespace {
+
+std::mutex g_noalloc_lock;
+unsigned char* g_noalloc_ptr[128];  // device address of the scratch, per device ordinal
+
+// Host code must not take the address of g_noalloc_scratch directly (that is
+// a host-side shadow); the device address is looked up once per device, with
+// that device current.
+er_status noalloc_scratch(int device, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_lock);
+  if (device < 0 || device >= 128) return fail(ER_ERR_INVALID_ARG, "device ordinal out of range");
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
+    g_noalloc_ptr[device] = (unsigned char*)p;
+  }
+  *out = g_noalloc_ptr[device];
+  return ER_OK;
+}
+
+WaveView noalloc_view(unsigned char* base, unsigned long long*& stats) {
+  WaveView w;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += pad256(bytes);
+    return p;
+  };
+  const int64_t N = kNoAllocPaths;
+  w.aov = false;
+  w.thr = (float4*)take(N * 16);
+  w.light = (float4*)take(N * 16);
+  w.pend = (float4*)take(N * 64);
+  w.vis = (uint8_t*)take(N * 2);
+  w.bounces = (int32_t*)take(N * 4);
+  w.q_o[0] = (float4*)take(N * 16);
+  w.q_d[0] = (float4*)take(N * 16);
+  w.q_o[1] = (float4*)take(N * 16);
+  w.q_d[1] = (float4*)take(N * 16);
+  w.hits = (float4*)take(N * 16);
+  w.s_o = (float4*)take(N * 32);
+  w.s_d = (float4*)take(N * 32);
+  w.s_p = (float4*)take(N * 32);
+  w.counts = (int32_t*)take(16 * 4);
+  stats = (unsigned long long*)take(16 * 8);
+  w.stats = stats;
+  w.shadow_half = N;
+  return w;
+}
+
+}  // namespace
+}  // namespace er
+
+extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, float* beauty, uint32_t* samples,
+                                       uint32_t* pathcount) {
+  er_status st = check_opts(s, o);
+  if (st != ER_OK) return st;
+  if (!beauty || !samples || !pathcount) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: NULL film buffer");
+  if ((uintptr_t)beauty % 16 != 0) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: beauty must be 16-byte aligned");
+  const uint32_t allowed = ER_RENDER_CONTINUE;
+  if (o->flags & ~allowed)
+    return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: only ER_RENDER_CONTINUE is supported");
+  const int32_t W = s->camera.x_res, H = s->camera.y_res;
+  const int64_t npix = (int64_t)W * H;
+  if (npix > kNoAllocPaths)
+    return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: " + std::to_string(npix) + " pixels exceed the limit of " +
+                                        std::to_string(kNoAllocPaths) + " (ER_NOALLOC_MAX_PATHS)");
+  unsigned char* base = nullptr;
+  if ((st = noalloc_scratch(s->device, &base)) != ER_OK) return st;
+  unsigned long long* stats = nullptr;
+  WaveView w = noalloc_view(base, stats);
+  Film F;
+  F.w = W;
+  F.h = H;
+  F.beauty = (float4*)beauty;
+  F.samples = samples;
+  F.pathcount = pathcount;
+  F.aov_on = false;
+  if (!(o->flags & ER_RENDER_CONTINUE)) {
+    k_film_clear<<<(unsigned)((npix + 255) / 256), 256, 0, s->stream>>>(F, (int32_t)npix);
+  }
+  const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
+  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : (int32_t)(kNoAllocPaths / npix);
+  sw = std::max(1, std::min(sw, (int32_t)(kNoAllocPaths / npix)));
+  WaveParams P;
+  P.W = W; P.H = H; P.npix = (int32_t)npix; P.max_depth = max_depth;
+  P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
+  P.flags = 0;
+  static int g_tr = 0, g_tr8 = 0, g_sh = 0;
+  if (!g_sh) {
+    g_tr = grid_for(k_trace<false, false>, kTravBlock, s->num_sms);
+    g_tr8 = grid_for(k_trace<true, false>, kTravBlock, s->num_sms);
+    g_sh = grid_for(k_shade, 128, s->num_sms);
+  }
+  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+    int32_t cur = std::min(sw, o->spp - s0);
+    P.spp_wave = cur;
+    P.sample_base = o->sample_begin + s0;
+    int32_t n = cur * (int32_t)npix;
+    k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);  // also zeroes the queue counters
+    for (int32_t b = 0; b <= max_depth; b++) {
+      if (s->dev.use_q8) k_trace<true, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word);
+      else k_trace<false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word);
+      if (b == max_depth) break;
+      k_shade<<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b);
+    }
+    k_accumulate<<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "er_render_noalloc launch");
+  return check_device_error(s);
 }
