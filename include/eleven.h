@@ -259,6 +259,14 @@ er_status er_render_noalloc(er_scene* scene, const er_render_opts* opts, float* 
 er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
                           float* radiance, int32_t* bounces);
 
+/* Environment sampling diagnostics: counts[i] = how many of the 2^24
+ * uniform values the reference's HDRI::binarySearch (HDRI.hpp:130-142) maps
+ * to texel i (its effective distribution is counts / 2^24), and the alias
+ * table ER_RENDER_ENV_ALIAS samples it with (column i is kept when a 32-bit
+ * coin is below thresh[i], else alias[i] is taken).  Arrays of env w*h
+ * entries; any may be NULL.  Builds the table on first use. */
+er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
+
 /* ----------------------------------------------------------------- trace -- */
 
 enum {

@@ -114,6 +114,17 @@ void orc_p_hdri_sample(const er_texture* t, const float* cdf, float radiance_sum
   }
 }
 
+/* Effective texel distribution of HDRI::binarySearch (HDRI.hpp:130-142)
+ * over the renderer's uniform grid r = k * 2^-24, k = 1..2^24: counts[t]
+ * receives how many k select texel t (counts has w*h entries, zeroed here). */
+void orc_p_hdri_counts(const float* cdf, int32_t n, uint32_t* counts) {
+  for (int32_t i = 0; i < n; i++) counts[i] = 0;
+  for (int64_t k = 0; k < ((int64_t)1 << 24); k++) {
+    int32_t t = orc_hdri_search(cdf, (float)(k + 1) * (1.0f / 16777216.0f), n);
+    if (t >= 0 && t < n) counts[t]++;
+  }
+}
+
 /* texture fetch by uv (nearest, with tile/offset), out 3 per item */
 void orc_p_tex_uv(const er_texture* t, int64_t n, const float* uv, float* out) {
   orc_tex x = {t->width, t->height, t->data, t->x_tile, t->y_tile, t->x_offset, t->y_offset};

@@ -50,7 +50,16 @@ def orc():
         _orc.orc_p_camera.argtypes = [C.POINTER(A.er_camera), C.c_int64, A.IP, A.FP, A.FP]
         _orc.orc_p_sample_u.argtypes = [C.c_void_p, C.c_int64, A.IP, C.c_int32, A.FP, A.FP]
         _orc.orc_p_philox.argtypes = [C.c_int64, A.UP, C.c_uint32, C.c_uint32, A.UP]
+        _orc.orc_p_hdri_counts.argtypes = [A.FP, C.c_int32, A.UP]
     return _orc
+
+
+def hdri_counts(cdf, n):
+    """Effective texel counts of the environment search over the 2^24 grid."""
+    cdf = _f(cdf)
+    counts = np.zeros(n, np.uint32)
+    orc().orc_p_hdri_counts(_ptr(cdf), n, _ptr(counts, A.UP))
+    return counts
 
 
 def ref():

@@ -114,8 +114,8 @@ struct DevScene {
   const er_point_light* lights;
   DevTex env;
   const float* cdf;      // env CDF, w*h+1 floats (HDRI.hpp:107-128)
-  const int32_t* alias_idx;   // env alias table (w*h) or null
-  const float* alias_prob;
+  const int32_t* alias_idx;   // env alias table (w*h) or null (env.cu)
+  const uint32_t* alias_thresh;
   float radiance_sum;
   int32_t n_lights;
   int32_t n_mats;
@@ -157,6 +157,7 @@ struct er_scene {
   unsigned long long* d_stats = nullptr;  // device ray counters
   std::vector<cudaEvent_t> ev_pool;       // per-launch profiling events
   std::vector<int> ev_stage;
+  const uint32_t* env_counts = nullptr;   // effective env texel counts (env.cu)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -167,4 +168,5 @@ DevCamera make_dev_camera(const er_camera& c);
 void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
+er_status build_env_alias(er_scene* s);
 }  // namespace er

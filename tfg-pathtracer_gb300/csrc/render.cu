@@ -299,7 +299,17 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
         float ndl = fabsf(dot(dir, hd.normal));
         // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked)
         const DevTex& E = S.env;
-        int32_t cnt = hdri_search(S.cdf, r1, E.w * E.h);
+        int32_t cnt;
+        if ((P.flags & ER_RENDER_ENV_ALIAS) && S.alias_idx) {
+          // O(1) draw from the search's effective distribution (env.cu):
+          // column from the shared light word, coin from a second word
+          uint32_t coin = philox(make_uint4(idx, (uint32_t)(P.sample_base + s), 2u + (uint32_t)bounce, 1u), P.k0,
+                                 P.k1).x;
+          int32_t col = (int32_t)__umulhi(rn.w, (uint32_t)(E.w * E.h));
+          cnt = coin < __ldg(S.alias_thresh + col) ? col : __ldg(S.alias_idx + col);
+        } else {
+          cnt = hdri_search(S.cdf, r1, E.w * E.h);
+        }
         float nu = __fdiv_rn((float)(cnt % E.w), (float)E.w), nv = __fdiv_rn((float)(cnt / E.w), (float)E.h);
         int32_t ix = __float2int_rz(nu * (float)E.w), iy = __float2int_rz(nv * (float)E.h);
         ix = __float2int_rz(E.x_tile * ((float)ix - E.x_offset * (float)E.w)) % E.w;
@@ -707,6 +717,7 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
   if (st != ER_OK) return st;
   const bool aov = o->flags & ER_RENDER_AOV;
   const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
+  if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
   if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
   unsigned long long st0[8];
   ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
@@ -763,6 +774,11 @@ extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float
   }
   er_render_opts oo = *o;
   oo.flags &= ~(uint32_t)ER_RENDER_AOV;
+  if ((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) {
+    cudaFree(d_rad);
+    cudaFree(d_b);
+    return st;
+  }
   st = run(s, &oo, d_rad, d_b, nullptr);
   if (st == ER_OK) {
     cudaMemcpyAsync(radiance, d_rad, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);

@@ -149,6 +149,6 @@ EXPORTED = [
     "er_status_string", "er_last_error", "er_abi_version",
     "er_scene_create", "er_scene_load", "er_scene_info_get",
     "er_scene_set_camera", "er_scene_get_camera", "er_scene_free",
-    "er_render", "er_film_read", "er_render_paths", "er_render_noalloc",
+    "er_render", "er_film_read", "er_render_paths", "er_render_noalloc", "er_env_distribution",
     "er_trace_closest", "er_encode_ldr", "er_write_image",
 ]
