@@ -267,6 +267,54 @@ er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
  * entries; any may be NULL.  Builds the table on first use. */
 er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
 
+/* ----------------------------------------------------------------- batch -- */
+/* Many scenes and views rendered together.  No counterpart in the
+ * reference, whose renderCuda (kernel.cu:665-686) renders one scene per
+ * process through device globals.  A batch merges the device data of its
+ * scenes (which must outlive it and stay unchanged); each job is a scene,
+ * a view and sample options; all jobs share wavefront queues, and one
+ * render is one captured CUDA graph.  Each job's film equals er_render's for
+ * the same scene, camera and options. */
+typedef struct er_batch er_batch;
+
+typedef struct er_batch_job {
+  int32_t scene;          /* index into the scenes given to er_batch_create */
+  int32_t spp;
+  int32_t max_depth;      /* <= 0: 5 */
+  int32_t sample_begin;
+  uint64_t seed;
+  uint32_t flags;         /* ER_RENDER_ENV_ALIAS, ER_RENDER_ACCUM_FP64 */
+  int32_t reserved;
+  er_camera camera;       /* the view; the film is camera.x_res x y_res */
+} er_batch_job;
+
+/* Schedule of a batch render (what er_batch_autotune searches). */
+typedef struct er_batch_tuning {
+  int32_t wave_paths;           /* paths per wave; 0 = 4,194,304; at least the largest job's pixels */
+  int32_t trace_blocks_per_sm;  /* persistent traversal grid = SMs x this; 0 = as many as fit */
+  int32_t shade_blocks_per_sm;  /* shading grid = SMs x this; 0 = as many as fit */
+  int32_t split_trace;          /* 1: extension, point-light and env rays as three traversal launches */
+  int32_t use_graph;            /* 1: capture the launch sequence once and replay it */
+  int32_t reserved[3];
+} er_batch_tuning;
+
+/* opts: bvh_format (ER_BVH_Q8 needs scenes built with it) and stream. */
+er_status er_batch_create(er_scene* const* scenes, int32_t n_scenes, const er_scene_opts* opts, er_batch** out);
+/* Replaces the job list (allocates each job's film). */
+er_status er_batch_set_jobs(er_batch* batch, const er_batch_job* jobs, int32_t n_jobs);
+/* Renders every job from a cleared film.  tuning NULL: the autotuned
+ * schedule if er_batch_autotune ran, else the defaults. */
+er_status er_batch_render(er_batch* batch, const er_batch_tuning* tuning, er_render_stats* stats);
+/* Film of one job: RGBA float beauty, per-pixel sample and path-vertex
+ * counts (flags: ER_RENDER_DEVICE_OUT for device destinations). */
+er_status er_batch_read(er_batch* batch, int32_t job, uint32_t flags, float* beauty, uint32_t* samples,
+                        uint32_t* pathcount);
+/* Times the current jobs under candidate schedules (best of reps renders
+ * each) and keeps the fastest for er_batch_render(batch, NULL, ...). */
+er_status er_batch_autotune(er_batch* batch, int32_t reps, er_batch_tuning* best);
+er_status er_batch_info(const er_batch* batch, int32_t* n_waves, int64_t* device_bytes);
+er_status er_batch_free(er_batch* batch);
+
 /* ----------------------------------------------------------------- trace -- */
 
 enum {

@@ -139,6 +139,59 @@ struct Film {
 
 struct Wave;  // wavefront buffers (render.cu)
 
+// Per-wave constants of the sample loop (one job's slice of samples).
+struct WaveParams {
+  int32_t W, H, npix, spp_wave, sample_base, max_depth;
+  uint32_t k0, k1;
+  uint32_t flags;
+};
+
+// ------------------------------------------------------------------ batch --
+//
+// A batch wave holds slices of several jobs: slice k owns the wave's paths
+// [path_base, path_base + spp_wave * npix) and accumulate items
+// [pix_base, pix_base + npix).  Jobs see one merged device scene; what
+// differs per job (BVH root, environment, lights, camera, film) comes from
+// the job table.
+struct BatchSeg {
+  int32_t path_base, pix_base, job, pad;
+  WaveParams P;
+};
+
+struct BatchJobDev {
+  DevTex env;
+  const float* cdf;
+  const int32_t* alias_idx;
+  const uint32_t* alias_thresh;
+  const er_point_light* lights;
+  float radiance_sum;
+  int32_t n_lights;
+  int32_t root;       // BVH root node in the merged node array
+  float scene_eps;
+  DevCamera cam;
+  Film film;
+};
+
+struct BatchView {
+  const BatchSeg* segs = nullptr;
+  const BatchJobDev* jobs = nullptr;
+  int32_t n_segs = 0;
+  int32_t n_acc = 0;
+};
+
+// One wave of a batch plan: segments [seg_begin, seg_begin + n_segs) of the
+// plan's device segment table.
+struct BatchWave {
+  int32_t seg_begin, n_segs, n_paths, n_acc, max_depth;
+};
+
+// Launch schedule knobs (the autotuner's search space).
+struct BatchSchedule {
+  int32_t trace_blocks_per_sm;  // 0 = as many as fit
+  int32_t shade_blocks_per_sm;  // 0 = as many as fit
+  bool split_trace;             // extension / point / env traversal as three launches
+};
+
 }  // namespace er
 
 struct er_scene {
@@ -158,6 +211,7 @@ struct er_scene {
   std::vector<cudaEvent_t> ev_pool;       // per-launch profiling events
   std::vector<int> ev_stage;
   const uint32_t* env_counts = nullptr;   // effective env texel counts (env.cu)
+  int64_t texel_count = 0;                // float4 entries of dev.texels (textures + env)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -169,4 +223,13 @@ void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
 er_status build_env_alias(er_scene* s);
+
+// Wavefront buffers for `cap` paths (render.cu); stats = device ray counters.
+er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out);
+void wave_destroy(Wave* w);
+er_status film_clear(const Film& F, cudaStream_t stream);
+// Launches every wave of a batch plan on `stream` (render.cu).
+er_status batch_launch(const DevScene& S, Wave* w, const BatchSeg* d_segs, const BatchJobDev* d_jobs,
+                       const std::vector<BatchWave>& waves, const BatchSchedule& sch, int num_sms, uint32_t* err,
+                       cudaStream_t stream, int64_t* launches);
 }  // namespace er

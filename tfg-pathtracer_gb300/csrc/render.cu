@@ -47,12 +47,6 @@ struct Wave {
   std::vector<void*> mem;
 };
 
-struct WaveParams {
-  int32_t W, H, npix, spp_wave, sample_base, max_depth;
-  uint32_t k0, k1;
-  uint32_t flags;
-};
-
 // Queue counters (w.counts), by bounce parity q = b & 1:
 //   kExt + q      extension rays of bounce b (written by raygen / shade(b-1))
 //   kEnv + q      env shadow rays of bounce b (written by shade(b))
@@ -84,23 +78,63 @@ __device__ __forceinline__ int32_t out_index(const WaveParams& P, int32_t x, int
   return P.W * (P.H - y - 1) + x;
 }
 
-__global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n) {
+// Batch slice of wave path p (slices are sorted by path_base).
+__device__ __forceinline__ int32_t find_seg(const BatchView& B, int32_t p) {
+  int32_t lo = 0, hi = B.n_segs - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(&B.segs[mid].path_base) <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Batch slice of accumulate item i.
+__device__ __forceinline__ int32_t find_seg_pix(const BatchView& B, int32_t i) {
+  int32_t lo = 0, hi = B.n_segs - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(&B.segs[mid].pix_base) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Path p's wave constants, index within its job's slice, and job (0 for a
+// single-scene render).  Queue entries carry the job in a spare lane so the
+// traversal can start at that job's BVH root.
+template <bool BATCH>
+__device__ __forceinline__ int32_t path_slice(const BatchView& B, int32_t p, WaveParams& P, int32_t& job) {
+  if (!BATCH) {
+    job = 0;
+    return p;
+  }
+  const BatchSeg& g = B.segs[find_seg(B, p)];
+  P = g.P;
+  job = g.job;
+  return p - g.path_base;
+}
+
+template <bool BATCH>
+__global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchView B) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p == 0) {
     for (int k = 0; k < 16; k++) w.counts[k] = 0;
     w.counts[kExt] = n;
   }
   if (p >= n) return;
-  int32_t pix = p % P.npix, s = p / P.npix;
+  int32_t job;
+  int32_t local = path_slice<BATCH>(B, p, P, job);
+  int32_t pix = local % P.npix, s = local / P.npix;
   int32_t x = pix % P.W, y = pix / P.W;
   uint32_t idx = (uint32_t)out_index(P, x, y);
   uint32_t sample = (uint32_t)(P.sample_base + s);
   uint4 a = philox(make_uint4(idx, sample, 0u, 0u), P.k0, P.k1);
   uint4 b = philox(make_uint4(idx, sample, 1u, 0u), P.k0, P.k1);
   f3 o, d;
-  camera_ray(S.cam, x, y, u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), o, d);
+  camera_ray(BATCH ? B.jobs[job].cam : S.cam, x, y, u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), o, d);
   w.q_o[0][p] = make_float4(o.x, o.y, o.z, __int_as_float(p));
-  w.q_d[0][p] = make_float4(d.x, d.y, d.z, 0.0f);
+  w.q_d[0][p] = make_float4(d.x, d.y, d.z, __int_as_float(job));
   w.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
   w.light[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   w.pend[4 * (size_t)p + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -129,17 +163,23 @@ __device__ __forceinline__ void flush_counts(unsigned long long* stats, int k, c
 // One traversal launch per bounce: the extension rays of bounce b (closest
 // hit) together with the shadow rays of bounce b-1, which are independent
 // of them.  Three persistent phases; every warp helps in all of them.
-template <bool Q8, bool STATS>
-__global__ void __launch_bounds__(kTravBlock, kTravMinBlocks) k_trace(DevScene S, WaveView w, int32_t b, uint32_t* err) {
+//
+// `phases` selects the phases (1 extension, 2 point-light, 4 env); a split
+// schedule runs them as three launches, the launch with phase 1 first.
+template <bool Q8, bool STATS, bool BATCH>
+__global__ void __launch_bounds__(kTravBlock, kTravMinBlocks)
+    k_trace(DevScene S, WaveView w, int32_t b, uint32_t* err, BatchView B, uint32_t phases) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
   const int32_t q = b & 1, qp = q ^ 1;
-  const int32_t n_ext = w.counts[kExt + q];
-  const int32_t n_pt = w.counts[kPt + qp];
-  const int32_t n_env = w.counts[kEnv + qp];
+  const int32_t n_ext = (phases & 1u) ? w.counts[kExt + q] : 0;
+  const int32_t n_pt = (phases & 2u) ? w.counts[kPt + qp] : 0;
+  const int32_t n_env = (phases & 4u) ? w.counts[kEnv + qp] : 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    w.counts[kExt + qp] = 0;  // shade(b) appends the next extension rays
-    w.counts[kEnv + q] = 0;   // ... and the shadow rays of bounce b
-    w.counts[kPt + q] = 0;
+    if (phases & 1u) {
+      w.counts[kExt + qp] = 0;  // shade(b) appends the next extension rays
+      w.counts[kEnv + q] = 0;   // ... and the shadow rays of bounce b
+      w.counts[kPt + q] = 0;
+    }
     atomicAdd(&w.stats[0], (unsigned long long)n_ext);
     atomicAdd(&w.stats[1], (unsigned long long)(n_env + n_pt));
   }
@@ -156,7 +196,12 @@ __global__ void __launch_bounds__(kTravBlock, kTravMinBlocks) k_trace(DevScene S
       S, n_ext, &w.counts[kClaim], stk + threadIdx.x, st, err,
       [&](int32_t i, auto& tr) {
         float4 a = qo[i], d = qd[i];
-        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+        if (BATCH) {
+          const BatchJobDev& J = B.jobs[__float_as_int(d.w)];
+          tr.init_at(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f, J.root, J.scene_eps);
+        } else {
+          tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+        }
       },
       [&](int32_t i, auto& tr) { hits[i] = make_float4(tr.t, tr.u, tr.v, __int_as_float(tr.slot)); });
   // point-light rays: shadow queue [half, half + n_pt)
@@ -164,7 +209,12 @@ __global__ void __launch_bounds__(kTravBlock, kTravMinBlocks) k_trace(DevScene S
       S, n_pt, &w.counts[kClaim + 1], stk + threadIdx.x, ss, err,
       [&](int32_t i, auto& tr) {
         float4 a = so[half + i], d = sd[half + i], p = spp[half + i];
-        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk(p.x, p.y, p.z), d.w);
+        if (BATCH) {
+          const BatchJobDev& J = B.jobs[__float_as_int(p.w)];
+          tr.init_at(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk(p.x, p.y, p.z), d.w, J.root, J.scene_eps);
+        } else {
+          tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk(p.x, p.y, p.z), d.w);
+        }
       },
       [&](int32_t i, auto& tr) { vis[__float_as_int(so[half + i].w)] = tr.occluded ? 0 : 1; });
   // env rays: shadow queue [0, n_env)
@@ -172,7 +222,12 @@ __global__ void __launch_bounds__(kTravBlock, kTravMinBlocks) k_trace(DevScene S
       S, n_env, &w.counts[kClaim + 2], stk + threadIdx.x, ss, err,
       [&](int32_t i, auto& tr) {
         float4 a = so[i], d = sd[i];
-        tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+        if (BATCH) {
+          const BatchJobDev& J = B.jobs[__float_as_int(d.w)];
+          tr.init_at(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f, J.root, J.scene_eps);
+        } else {
+          tr.init(S, mk(a.x, a.y, a.z), mk(d.x, d.y, d.z), mk1(0.f), 0.f);
+        }
       },
       [&](int32_t i, auto& tr) { vis[__float_as_int(so[i].w)] = tr.occluded ? 0 : 1; });
   if (STATS) {
@@ -201,7 +256,8 @@ __device__ __forceinline__ void resolve(const WaveView& w, int32_t p, float4& L)
   w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
 }
 
-__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParams P, int32_t bounce) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B) {
   const int32_t qin = bounce & 1;
   const int32_t n = w.counts[kExt + qin];
   const float4* qo = w.q_o[qin];
@@ -212,7 +268,6 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
     w.counts[kClaim + 1] = 0;
     w.counts[kClaim + 2] = 0;
   }
-  const bool last = bounce + 1 >= P.max_depth;
   for (int32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     int32_t i = base + threadIdx.x;
     bool valid = i < n;
@@ -220,10 +275,25 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
     f3 next_o = mk1(0), next_d = mk1(0), env_o = mk1(0), env_d = mk1(0), pt_o = mk1(0), pt_d = mk1(0),
        pt_p = mk1(0);
     float pt_dist = 0.f;
-    int32_t p = 0;
+    int32_t p = 0, job = 0;
     if (valid) {
       float4 a = qo[i], b = qd[i];
       p = __float_as_int(a.w);
+      // the path's job: its wave constants and the per-scene parts of S
+      WaveParams P = P0;
+      DevScene S = S0;
+      int32_t local = path_slice<BATCH>(B, p, P, job);
+      if (BATCH) {
+        const BatchJobDev& J = B.jobs[job];
+        S.env = J.env;
+        S.cdf = J.cdf;
+        S.alias_idx = J.alias_idx;
+        S.alias_thresh = J.alias_thresh;
+        S.lights = J.lights;
+        S.radiance_sum = J.radiance_sum;
+        S.n_lights = J.n_lights;
+      }
+      const bool last = bounce + 1 >= P.max_depth;
       f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
       float4 L = w.light[p];
       resolve(w, p, L);
@@ -287,7 +357,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
         hd.subsurface = M.subsurface;
         hd.sheen = M.sheen;
 
-        int32_t pix = p % P.npix, s = p / P.npix;
+        int32_t pix = local % P.npix, s = local / P.npix;
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         uint4 rn = philox(make_uint4(idx, (uint32_t)(P.sample_base + s), 2u + (uint32_t)bounce, 0u), P.k0, P.k1);
         DisneyCtx C = disney_ctx(hd, d);
@@ -373,31 +443,40 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveView w, WaveParam
     int32_t j = warp_append(&w.counts[kExt + qout], push_next);
     if (push_next) {
       w.q_o[qout][j] = make_float4(next_o.x, next_o.y, next_o.z, __int_as_float(p));
-      w.q_d[qout][j] = make_float4(next_d.x, next_d.y, next_d.z, 0.f);
+      w.q_d[qout][j] = make_float4(next_d.x, next_d.y, next_d.z, __int_as_float(job));
     }
     int32_t k = warp_append(&w.counts[kEnv + qin], push_env);
     if (push_env) {
       w.s_o[k] = make_float4(env_o.x, env_o.y, env_o.z, __int_as_float(2 * p));
-      w.s_d[k] = make_float4(env_d.x, env_d.y, env_d.z, 0.f);
+      w.s_d[k] = make_float4(env_d.x, env_d.y, env_d.z, __int_as_float(job));
     }
     k = warp_append(&w.counts[kPt + qin], push_pt);
     if (push_pt) {
       int64_t j = w.shadow_half + k;
       w.s_o[j] = make_float4(pt_o.x, pt_o.y, pt_o.z, __int_as_float(2 * p + 1));
       w.s_d[j] = make_float4(pt_d.x, pt_d.y, pt_d.z, pt_dist);
-      w.s_p[j] = make_float4(pt_p.x, pt_p.y, pt_p.z, 0.f);
+      w.s_p[j] = make_float4(pt_p.x, pt_p.y, pt_p.z, __int_as_float(job));
     }
   }
 }
 
 // kernel.cu:445-478 per pixel, samples in index order.
 __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WaveParams& P, const Film& F, int32_t sw,
-                                                 int32_t pix, uint32_t& bounce_sum);
+                                                 int32_t pix, int32_t path_base, uint32_t& bounce_sum);
 
-__global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw) {
+// One item per pixel of every slice (a single render: one slice).
+template <bool BATCH>
+__global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw, BatchView B) {
   int32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t bsum = 0;
-  if (pix < P.npix) accumulate_pixel(w, P, F, sw, pix, bsum);
+  if (BATCH) {
+    if (pix < B.n_acc) {
+      const BatchSeg& g = B.segs[find_seg_pix(B, pix)];
+      accumulate_pixel(w, g.P, B.jobs[g.job].film, g.P.spp_wave, pix - g.pix_base, g.path_base, bsum);
+    }
+  } else if (pix < P.npix) {
+    accumulate_pixel(w, P, F, sw, pix, 0, bsum);
+  }
   // path-vertex counter (the reference's kPaths numerator), one atomic per warp
   unsigned long long v = bsum;
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
@@ -405,7 +484,7 @@ __global__ void k_accumulate(WaveView w, WaveParams P, Film F, int32_t sw) {
 }
 
 __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WaveParams& P, const Film& F, int32_t sw,
-                                                 int32_t pix, uint32_t& bounce_sum) {
+                                                 int32_t pix, int32_t path_base, uint32_t& bounce_sum) {
   int32_t x = pix % P.W, y = pix / P.W;
   int32_t idx = out_index(P, x, y);
   uint32_t sa = F.samples[idx], pc = F.pathcount[idx];
@@ -416,7 +495,7 @@ __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WavePa
   float4 a[3];
   if (F.aov_on) for (int k = 0; k < 3; k++) a[k] = F.aov[k][idx];
   for (int32_t s = 0; s < sw; s++) {
-    int32_t p = s * P.npix + pix;
+    int32_t p = path_base + s * P.npix + pix;
     float4 L = w.light[p];
     resolve(w, p, L);
     pc += (uint32_t)w.bounces[p];
@@ -488,7 +567,7 @@ int grid_for(K kernel, int block, int sms) {
   return std::max(1, nb) * sms;
 }
 
-er_status alloc_w(er_scene* s, Wave* w, void** p, size_t bytes) {
+er_status alloc_w(Wave* w, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -498,19 +577,17 @@ er_status alloc_w(er_scene* s, Wave* w, void** p, size_t bytes) {
   return ER_OK;
 }
 
-er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
-  if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov)) return ER_OK;
-  free_wave(s);
-  Wave* ww = new Wave();
-  s->wave = ww;
+// Allocates the buffers of `ww` for `cap` paths; on failure the caller
+// frees what was allocated.
+er_status wave_fill(Wave* ww, int64_t cap, bool aov, unsigned long long* stats) {
   ww->cap = cap;
   WaveView* w = &ww->v;
   w->aov = aov;
-  w->stats = s->d_stats;
+  w->stats = stats;
   w->shadow_half = cap;
   er_status st;
 #define AL(ptr, bytes) \
-  if ((st = alloc_w(s, ww, (void**)&(ptr), (bytes))) != ER_OK) { free_wave(s); return st; }
+  if ((st = alloc_w(ww, (void**)&(ptr), (bytes))) != ER_OK) return st;
   AL(w->thr, cap * sizeof(float4));
   AL(w->light, cap * sizeof(float4));
   AL(w->pend, 4 * cap * sizeof(float4));
@@ -528,6 +605,15 @@ er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
   AL(w->counts, 16 * sizeof(int32_t));
 #undef AL
   return ER_OK;
+}
+
+er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
+  if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov)) return ER_OK;
+  free_wave(s);
+  s->wave = new Wave();
+  er_status st = wave_fill(s->wave, cap, aov, s->d_stats);
+  if (st != ER_OK) free_wave(s);
+  return st;
 }
 
 er_status ensure_film(er_scene* s, bool aov, bool fp64, bool clear) {
@@ -594,12 +680,13 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   const bool prof = o->flags & ER_RENDER_PROFILE;
   static int g_tr[4] = {0}, g_shade = 0;
   if (!g_shade) {
-    g_tr[0] = grid_for(k_trace<false, false>, kTravBlock, s->num_sms);
-    g_tr[1] = grid_for(k_trace<true, false>, kTravBlock, s->num_sms);
-    g_tr[2] = grid_for(k_trace<false, true>, kTravBlock, s->num_sms);
-    g_tr[3] = grid_for(k_trace<true, true>, kTravBlock, s->num_sms);
-    g_shade = grid_for(k_shade, 128, s->num_sms);
+    g_tr[0] = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
+    g_tr[1] = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
+    g_tr[2] = grid_for(k_trace<false, true, false>, kTravBlock, s->num_sms);
+    g_tr[3] = grid_for(k_trace<true, true, false>, kTravBlock, s->num_sms);
+    g_shade = grid_for(k_shade<false>, 128, s->num_sms);
   }
+  const BatchView NB;
   const int variant = (q8 ? 1 : 0) + (count ? 2 : 0);
   int64_t nl = 0;
   // Profiling: one event after every launch, attributed to its stage.
@@ -630,27 +717,28 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * npix;
-    k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);
+    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB);
     if ((st = mark(ER_STAGE_RAYGEN)) != ER_OK) return st;
     // trace(b): extension rays of bounce b + shadow rays of bounce b-1;
     // the extra trace(max_depth) finishes the last bounce's shadow rays.
     for (int32_t b = 0; b <= max_depth; b++) {
+      uint32_t* err = s->err_word;
       switch (variant) {
-        case 0: k_trace<false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
-        case 1: k_trace<true, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
-        case 2: k_trace<false, true><<<g_tr[2], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
-        default: k_trace<true, true><<<g_tr[3], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word); break;
+        case 0: k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
+        case 1: k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
+        case 2: k_trace<false, true, false><<<g_tr[2], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
+        default: k_trace<true, true, false><<<g_tr[3], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
       }
       if ((st = mark(ER_STAGE_TRACE)) != ER_OK) return st;
       if (b == max_depth) break;
-      k_shade<<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b);
+      k_shade<false><<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b, NB);
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
     }
     if (dump_rad) {
       k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, dump_rad, dump_b);
     } else {
       Film F = s->film;
-      k_accumulate<<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur);
+      k_accumulate<false><<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur, NB);
     }
     if ((st = mark(ER_STAGE_ACCUMULATE)) != ER_OK) return st;
     ER_CUDA(cudaGetLastError());
@@ -684,6 +772,91 @@ void free_film(er_scene* s) {
   cudaFree(F.samples);
   cudaFree(F.pathcount);
   F = Film();
+}
+
+er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out) {
+  Wave* ww = new Wave();
+  er_status st = wave_fill(ww, cap, false, stats);
+  if (st != ER_OK) {
+    wave_destroy(ww);
+    return st;
+  }
+  *out = ww;
+  return ER_OK;
+}
+
+void wave_destroy(Wave* w) {
+  if (!w) return;
+  for (void* p : w->mem) cudaFree(p);
+  delete w;
+}
+
+er_status film_clear(const Film& F, cudaStream_t stream) {
+  int32_t npix = F.w * F.h;
+  if (npix <= 0) return ER_OK;
+  k_film_clear<<<(npix + 255) / 256, 256, 0, stream>>>(F, npix);
+  ER_CUDA(cudaGetLastError());
+  return ER_OK;
+}
+
+// The batch's launch sequence: per wave raygen, max_depth + 1 traversal
+// launches (three each in a split schedule), max_depth shade launches and
+// one accumulate launch.  Slices of one job across waves are accumulated in
+// sample order, so each job's film equals a single-scene render's.
+er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, const BatchJobDev* d_jobs,
+                       const std::vector<BatchWave>& waves, const BatchSchedule& sch, int num_sms, uint32_t* err,
+                       cudaStream_t stream, int64_t* launches) {
+  static int occ_tr[2] = {0, 0}, occ_sh = 0;  // resident blocks per SM
+  if (!occ_sh) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tr[0], k_trace<false, false, true>, kTravBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tr[1], k_trace<true, false, true>, kTravBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_sh, k_shade<true>, 128, 0);
+    occ_tr[0] = std::max(1, occ_tr[0]);
+    occ_tr[1] = std::max(1, occ_tr[1]);
+    occ_sh = std::max(1, occ_sh);
+  }
+  const int q8 = S.use_q8 ? 1 : 0;
+  const int tb = sch.trace_blocks_per_sm > 0 ? std::min(sch.trace_blocks_per_sm, occ_tr[q8]) : occ_tr[q8];
+  const int sb = sch.shade_blocks_per_sm > 0 ? std::min(sch.shade_blocks_per_sm, occ_sh) : occ_sh;
+  const int g_tr = tb * num_sms, g_sh = sb * num_sms;
+  if (launches) *launches = 0;
+  if (waves.empty()) return ER_OK;  // (also: occupancy queries done before any stream capture)
+  const WaveView& w = wv->v;
+  const WaveParams P0{};
+  int64_t nl = 0;
+  auto trace = [&](int32_t b, const BatchView& B, uint32_t phases) {
+    if (q8) k_trace<true, false, true><<<g_tr, kTravBlock, 0, stream>>>(S, w, b, err, B, phases);
+    else k_trace<false, false, true><<<g_tr, kTravBlock, 0, stream>>>(S, w, b, err, B, phases);
+    nl++;
+  };
+  for (const BatchWave& bw : waves) {
+    if (bw.n_paths > wv->cap) return fail(ER_ERR_INVALID_ARG, "batch wave larger than its buffers");
+    BatchView B;
+    B.segs = d_segs + bw.seg_begin;
+    B.jobs = d_jobs;
+    B.n_segs = bw.n_segs;
+    B.n_acc = bw.n_acc;
+    const int32_t n = bw.n_paths;
+    k_raygen<true><<<(n + 255) / 256, 256, 0, stream>>>(S, w, P0, n, B);
+    nl++;
+    for (int32_t b = 0; b <= bw.max_depth; b++) {
+      if (sch.split_trace) {
+        trace(b, B, 1u);
+        trace(b, B, 2u);
+        trace(b, B, 4u);
+      } else {
+        trace(b, B, 7u);
+      }
+      if (b == bw.max_depth) break;
+      k_shade<true><<<g_sh, 128, 0, stream>>>(S, w, P0, b, B);
+      nl++;
+    }
+    k_accumulate<true><<<(bw.n_acc + 127) / 128, 128, 0, stream>>>(w, P0, Film(), 0, B);
+    nl++;
+  }
+  ER_CUDA(cudaGetLastError());
+  if (launches) *launches = nl;
+  return ER_OK;
 }
 
 }  // namespace er
@@ -917,23 +1090,26 @@ extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, flo
   P.flags = 0;
   static int g_tr = 0, g_tr8 = 0, g_sh = 0;
   if (!g_sh) {
-    g_tr = grid_for(k_trace<false, false>, kTravBlock, s->num_sms);
-    g_tr8 = grid_for(k_trace<true, false>, kTravBlock, s->num_sms);
-    g_sh = grid_for(k_shade, 128, s->num_sms);
+    g_tr = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
+    g_tr8 = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
+    g_sh = grid_for(k_shade<false>, 128, s->num_sms);
   }
+  const BatchView NB;
   for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
     int32_t cur = std::min(sw, o->spp - s0);
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * (int32_t)npix;
-    k_raygen<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n);  // also zeroes the queue counters
+    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB);  // also zeroes the queue counters
     for (int32_t b = 0; b <= max_depth; b++) {
-      if (s->dev.use_q8) k_trace<true, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word);
-      else k_trace<false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word);
+      if (s->dev.use_q8)
+        k_trace<true, false, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+      else
+        k_trace<false, false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
       if (b == max_depth) break;
-      k_shade<<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b);
+      k_shade<false><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB);
     }
-    k_accumulate<<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur);
+    k_accumulate<false><<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur, NB);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "er_render_noalloc launch");

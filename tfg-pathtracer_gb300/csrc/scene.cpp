@@ -329,6 +329,7 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   S.scene_eps = ext;
   S.use_q8 = o.bvh_format == ER_BVH_Q8;
   S.cam = make_dev_camera(d->camera);
+  s->texel_count = (int64_t)pool.size();
   s->err_word = (uint32_t*)p_err;
   s->d_stats = (unsigned long long*)((char*)p_err + 64);
 

@@ -130,6 +130,13 @@ struct Traverser {
   }
 
   __device__ __forceinline__ void init(const DevScene& S, f3 o_, f3 d_, f3 pp_, float pdist_) {
+    init_at(S, o_, d_, pp_, pdist_, 0, S.scene_eps);
+  }
+
+  // Starts at node `root` of a merged node array (a batch of scenes), with
+  // that scene's coordinate extent `eps`.
+  __device__ __forceinline__ void init_at(const DevScene& S, f3 o_, f3 d_, f3 pp_, float pdist_, int32_t root,
+                                          float eps) {
     o = o_;
     d = d_;
     pp = pp_;
@@ -141,14 +148,14 @@ struct Traverser {
     inv = mk(d.x != 0.0f ? __frcp_rn(d.x) : copysignf(big, d.x), d.y != 0.0f ? __frcp_rn(d.y) : copysignf(big, d.y),
              d.z != 0.0f ? __frcp_rn(d.z) : copysignf(big, d.z));
     float omax = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
-    slack = (omax + S.scene_eps) * 2.0e-6f;
+    slack = (omax + eps) * 2.0e-6f;
     // |error| of fma(plane, inv, -o*inv) <= (|o| + |plane|) |inv| 2^-23;
     // node planes lie within +-scene_eps.  Margin: 4x that.  It only widens
     // slabs whose plane lies within ~1e-5 (|o| + scene_eps) of the origin.
     const float k = 4.76837158e-7f;  // 2^-21
-    float mx = (fabsf(o.x) + S.scene_eps) * fabsf(inv.x) * k;
-    float my = (fabsf(o.y) + S.scene_eps) * fabsf(inv.y) * k;
-    float mz = (fabsf(o.z) + S.scene_eps) * fabsf(inv.z) * k;
+    float mx = (fabsf(o.x) + eps) * fabsf(inv.x) * k;
+    float my = (fabsf(o.y) + eps) * fabsf(inv.y) * k;
+    float mz = (fabsf(o.z) + eps) * fabsf(inv.z) * k;
     f3 oi = mk(-(o.x * inv.x), -(o.y * inv.y), -(o.z * inv.z));
     bnear = mk(oi.x - mx, oi.y - my, oi.z - mz);
     bfar = mk(oi.x + mx, oi.y + my, oi.z + mz);
@@ -164,7 +171,7 @@ struct Traverser {
     occluded = false;
     done = false;
     sp = 0;
-    node = 0;
+    node = root;
     leaf = 0;
     leaf_key = 0.0f;
     // a ray visits every node at most once; a longer walk means a corrupt tree
@@ -358,6 +365,9 @@ constexpr int kRefillThreshold = ER_REFILL_THRESHOLD;
 template <int MODE, bool Q8, bool STATS, typename Load, typename Store>
 __device__ __forceinline__ void persistent_traverse(const DevScene& S, int32_t n, int32_t* counter, int2* sstk,
                                                     TravStats& st, uint32_t* err, Load load, Store store) {
+  // An empty queue claims nothing, so its counter stays zero for a later
+  // launch of the same phase.
+  if (n <= 0) return;
   int2 lstk[kLocalStack];
   Traverser<MODE, Q8, STATS> tr;
   const unsigned lane = threadIdx.x & 31u;

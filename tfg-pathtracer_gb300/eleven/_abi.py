@@ -144,11 +144,29 @@ class er_trace_stats(C.Structure):
     ]
 
 
+class er_batch_job(C.Structure):
+    _fields_ = [
+        ("scene", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
+        ("sample_begin", C.c_int32), ("seed", C.c_uint64), ("flags", C.c_uint32),
+        ("reserved", C.c_int32), ("camera", er_camera),
+    ]
+
+
+class er_batch_tuning(C.Structure):
+    _fields_ = [
+        ("wave_paths", C.c_int32), ("trace_blocks_per_sm", C.c_int32),
+        ("shade_blocks_per_sm", C.c_int32), ("split_trace", C.c_int32),
+        ("use_graph", C.c_int32), ("reserved", C.c_int32 * 3),
+    ]
+
+
 # Every symbol include/eleven.h declares (checked by the CPU tests).
 EXPORTED = [
     "er_status_string", "er_last_error", "er_abi_version",
     "er_scene_create", "er_scene_load", "er_scene_info_get",
     "er_scene_set_camera", "er_scene_get_camera", "er_scene_free",
     "er_render", "er_film_read", "er_render_paths", "er_render_noalloc", "er_env_distribution",
+    "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
+    "er_batch_autotune", "er_batch_info", "er_batch_free",
     "er_trace_closest", "er_encode_ldr", "er_write_image",
 ]

@@ -67,6 +67,21 @@ def load(build_if_missing=True):
     L.er_render_noalloc.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_render_paths.restype = A.er_status
     L.er_render_paths.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p]
+    L.er_batch_create.restype = A.er_status
+    L.er_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(A.er_scene_opts),
+                                  C.POINTER(C.c_void_p)]
+    L.er_batch_set_jobs.restype = A.er_status
+    L.er_batch_set_jobs.argtypes = [C.c_void_p, C.POINTER(A.er_batch_job), C.c_int32]
+    L.er_batch_render.restype = A.er_status
+    L.er_batch_render.argtypes = [C.c_void_p, C.POINTER(A.er_batch_tuning), C.POINTER(A.er_render_stats)]
+    L.er_batch_read.restype = A.er_status
+    L.er_batch_read.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.er_batch_autotune.restype = A.er_status
+    L.er_batch_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(A.er_batch_tuning)]
+    L.er_batch_info.restype = A.er_status
+    L.er_batch_info.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    L.er_batch_free.restype = A.er_status
+    L.er_batch_free.argtypes = [C.c_void_p]
     L.er_trace_closest.restype = A.er_status
     L.er_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_uint32, C.POINTER(A.er_trace_stats)]
@@ -179,6 +194,76 @@ class Scene:
         b = np.zeros((spp, H * W), np.int32)
         check(load().er_render_paths(self.h, C.byref(o), _p(rad), _p(b)), "er_render_paths")
         return rad, b
+
+
+class Batch:
+    """Several scenes and views rendered together (er_batch).
+
+    jobs: dicts with scene (index), spp, max_depth, seed, camera (er_camera
+    or None for that scene's own camera), optional sample_begin and flags.
+    """
+
+    def __init__(self, scenes, bvh_format=A.ER_BVH_FP32):
+        L = load()
+        self.scenes = list(scenes)  # kept alive: the batch reads their device data
+        arr = (C.c_void_p * len(self.scenes))(*[s.h for s in self.scenes])
+        opts = A.er_scene_opts(bvh_format, 0, 0, None)
+        h = C.c_void_p()
+        check(L.er_batch_create(arr, len(self.scenes), C.byref(opts), C.byref(h)), "er_batch_create")
+        self.h = h
+        self.jobs = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().er_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_jobs(self, jobs):
+        arr = (A.er_batch_job * len(jobs))()
+        for k, j in enumerate(jobs):
+            cam = j.get("camera") or self.scenes[j["scene"]].camera()
+            arr[k] = A.er_batch_job(j["scene"], j["spp"], j.get("max_depth", 5), j.get("sample_begin", 0),
+                                    j.get("seed", 0), j.get("flags", 0), 0, cam)
+        check(load().er_batch_set_jobs(self.h, arr, len(jobs)), "er_batch_set_jobs")
+        self.jobs = [dict(j, camera=arr[k].camera) for k, j in enumerate(jobs)]
+
+    def render(self, tuning=None):
+        st = A.er_render_stats()
+        t = C.byref(tuning) if tuning is not None else None
+        check(load().er_batch_render(self.h, t, C.byref(st)), "er_batch_render")
+        return st
+
+    def read(self, job):
+        cam = self.jobs[job]["camera"]
+        n = int(cam.x_res) * int(cam.y_res)
+        beauty = np.zeros((n, 4), np.float32)
+        samples = np.zeros(n, np.uint32)
+        pc = np.zeros(n, np.uint32)
+        check(load().er_batch_read(self.h, job, 0, _p(beauty), _p(samples), _p(pc)), "er_batch_read")
+        return dict(beauty=beauty, samples=samples, pathcount=pc)
+
+    def autotune(self, reps=2):
+        t = A.er_batch_tuning()
+        check(load().er_batch_autotune(self.h, reps, C.byref(t)), "er_batch_autotune")
+        return t
+
+    def info(self):
+        nw = C.c_int32(0)
+        nb = C.c_int64(0)
+        check(load().er_batch_info(self.h, C.byref(nw), C.byref(nb)), "er_batch_info")
+        return int(nw.value), int(nb.value)
 
 
 def encode_ldr(rgba, width, height):

@@ -468,6 +468,60 @@ def config1(x_res=1920, y_res=1080, seed=1, n_meshes=200, tri_lo=1000, tri_hi=20
                        env=lognormal_env(env_w, env_h, seed), name="c1")
 
 
+C2_RESOLUTIONS = [(128, 128), (256, 256), (320, 240), (512, 512), (640, 480), (800, 600), (1024, 768)]
+
+
+def displaced_spheres(n_tris, seed, x_res, y_res, n_lights, env_w=512, env_h=256, mesh_tris=8000):
+    """A scene of seeded value-noise-displaced UV spheres with about n_tris
+    triangles in total (meshes of about mesh_tris), Disney parameters as in
+    the 1M-triangle scene (no textures), n_lights point lights and a
+    log-normal environment of env_w x env_h."""
+    rng = np.random.default_rng(seed)
+    n_meshes = int(min(64, max(2, round(n_tris / mesh_tris))))
+    per = n_tris / n_meshes
+    meshes, mats = [], []
+    for i in range(n_meshes):
+        n_lat = max(3, int(round(math.sqrt(per / 4.0))))
+        v, f = uv_sphere(n_lat, 2 * n_lat)
+        disp = 1.0 + 0.2 * value_noise3(v * 2.0, seed * 7919 + i, octaves=3)
+        r = rng.uniform(0.4, 1.2)
+        c = np.array([rng.uniform(-7, 7), rng.uniform(-3, 3), rng.uniform(-4, 8)])
+        vd = v * disp[:, None] * r + c
+        meshes.append((vd, f, vertex_normals(vd, f), sphere_uv(v)))
+        mats.append(dict(albedo=tuple(rng.uniform(0, 1, 3)), roughness=rng.uniform(0.05, 1.0),
+                         metallic=float(rng.uniform() < 0.3), specular=0.5, clearcoat=rng.uniform(0, 1),
+                         sheen=rng.uniform(0, 1)))
+    P, N, U, O = _assemble(meshes)
+    cam = dict(x_res=x_res, y_res=y_res, focal_length=pinhole_focal(50.0), position=(0.0, 0.5, -16.0),
+               rotation=(0.0, 0.0, 0.0), bokeh=False)
+    pos = rng.uniform([-8, 4, -8], [8, 10, 8], (n_lights, 3))
+    rad = rng.uniform(30, 90, (n_lights, 3))
+    lights = np.stack([pos, rad], 1).astype(np.float32)
+    return SceneArrays(camera=cam, positions=P, normals=N, uvs=U, tri_object=O,
+                       object_material=np.arange(len(meshes), dtype=np.int32), materials=mats,
+                       lights=lights, env=lognormal_env(env_w, env_h, seed, sun=8), name=f"c2-{seed}")
+
+
+def config2(n_jobs=64, seed=2, tri_lo=10_000, tri_hi=500_000, resolutions=C2_RESOLUTIONS, spps=(4, 16, 64),
+            depths=(4, 8), env_w=512, env_h=256):
+    """Batching: n_jobs heterogeneous scenes/views.  Per job: resolution
+    uniform over `resolutions`, spp uniform over `spps`, max depth uniform in
+    depths[0]..depths[1], triangle count log-uniform in [tri_lo, tri_hi]
+    (displaced spheres), 1-4 point lights, a log-normal environment.
+    Returns (scene arrays, job dicts) with job["scene"] = its scene index."""
+    rng = np.random.default_rng(seed)
+    arrays, jobs = [], []
+    for j in range(n_jobs):
+        W, H = resolutions[int(rng.integers(len(resolutions)))]
+        spp = int(spps[int(rng.integers(len(spps)))])
+        depth = int(rng.integers(depths[0], depths[1] + 1))
+        tris = math.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi)))
+        n_lights = int(rng.integers(1, 5))
+        arrays.append(displaced_spheres(tris, seed * 1000 + j, W, H, n_lights, env_w, env_h))
+        jobs.append(dict(scene=j, spp=spp, max_depth=depth, seed=j))
+    return arrays, jobs
+
+
 def random_rays(scene, n, seed=3):
     """Origins uniform in the scene bounds, directions uniform on the sphere
     (z = 1-2u, phi = 2 pi v)."""
