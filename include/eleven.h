@@ -147,6 +147,9 @@ typedef struct er_scene_info {
   float max_shading_offset; /* bound on |shading position - geometric hit| */
   int32_t bvh_depth;
   int32_t bvh_format;
+  int32_t material_count;
+  int32_t env_width, env_height;
+  int32_t reserved;
 } er_scene_info;
 
 /* Build a scene from arrays (the harness / generator path). */
@@ -266,6 +269,32 @@ er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
  * coin is below thresh[i], else alias[i] is taken).  Arrays of env w*h
  * entries; any may be NULL.  Builds the table on first use. */
 er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
+
+/* --------------------------------------------------------------- adjoint -- */
+/* Differentiable parameters (no counterpart in the reference): per material
+ * 5 floats (albedo r, g, b, roughness, metallic, before the 2.2 power of
+ * kernel.cu:103-104) and the environment's texels (w*h*3 floats, storage
+ * order).  flags: ER_RENDER_DEVICE_OUT for device arrays.  Setting the
+ * environment rebuilds its CDF (HDRI.hpp:107-128). */
+er_status er_scene_get_params(er_scene* scene, float* materials, float* env);
+er_status er_scene_set_params(er_scene* scene, const float* materials, const float* env, uint32_t flags);
+
+/* Forward render by path replay: sampling (directions, pdfs, MIS weights,
+ * chosen texel and light) from the scene's parameters, BRDF values and
+ * environment radiance from eval_materials / eval_env (NULL = the scene's).
+ * With both NULL the film equals er_render's for the same options.  Only
+ * ER_RENDER_DEVICE_OUT and ER_RENDER_ENV_ALIAS apply. */
+er_status er_render_replay(er_scene* scene, const er_render_opts* opts, const float* eval_materials,
+                           const float* eval_env, float* beauty, uint32_t* samples, uint32_t* pathcount);
+
+/* Gradient of a loss with respect to the parameters, by path replay of the
+ * samples er_render made with the same opts: d_beauty = d loss / d beauty
+ * (W*H*4 floats, the film's layout), samples = that render's per-pixel
+ * sample counts.  The derivative holds the sampling fixed (the detached
+ * estimator er_render_replay evaluates).  Outputs: n_materials*5 and
+ * env w*h*3 floats. */
+er_status er_backward(er_scene* scene, const er_render_opts* opts, const float* d_beauty, const uint32_t* samples,
+                      float* grad_materials, float* grad_env, er_render_stats* stats);
 
 /* ----------------------------------------------------------------- batch -- */
 /* Many scenes and views rendered together.  No counterpart in the

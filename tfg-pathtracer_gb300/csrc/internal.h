@@ -223,6 +223,8 @@ void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
 er_status build_env_alias(er_scene* s);
+// Environment CDF and radiance sum as the reference builds them (scene.cpp).
+void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum);
 
 // Wavefront buffers for `cap` paths (render.cu); stats = device ray counters.
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out);

@@ -18,6 +18,7 @@
 #include "internal.h"
 #include "shade.cuh"
 #include "traverse.cuh"
+#include "vertex.cuh"
 
 namespace er {
 
@@ -303,138 +304,42 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WavePara
       int32_t slot = __float_as_int(h.w);
       if (slot < 0) {
         // kernel.cu:414-419: environment on escape, no MIS weight
-        float eu, ev;
-        spherical_mapping(-d, eu, ev);
-        f3 e = tex_uv(S, S.env, eu, ev);
+        f3 e = escape_radiance(S, d, nullptr);
         L.x = __fadd_rn(L.x, __fmul_rn(e.x, thr.x));
         L.y = __fadd_rn(L.y, __fmul_rn(e.y, thr.y));
         L.z = __fadd_rn(L.z, __fmul_rn(e.z, thr.z));
         w.bounces[p] = bounce;
       } else {
-        // Tri.hpp:70-92 + 153-157 rebuilt from (t, u, v) with the same ops
-        const float4* tv = S.tri_v + 3 * (size_t)slot;
-        const float4* tn = S.tri_n + 3 * (size_t)slot;
-        float4 v0 = __ldg(tv), v1 = __ldg(tv + 1), v2 = __ldg(tv + 2);
-        float4 n0 = __ldg(tn), n1 = __ldg(tn + 1), n2 = __ldg(tn + 2);
-        float t = h.x, u = h.y, v = h.z;
-        f3 sn;
-        f3 pos = ref_position(o, d, t, u, v, from4(v0), from4(v1), from4(v2), from4(n0), from4(n1), from4(n2), &sn);
-        const float2* tuv = S.tri_uv + 3 * (size_t)slot;
-        float2 uv0 = __ldg(tuv), uv1 = __ldg(tuv + 1), uv2 = __ldg(tuv + 2);
-        float tu = __fadd_rn(__fadd_rn(uv0.x, __fmul_rn(__fsub_rn(uv1.x, uv0.x), u)), __fmul_rn(__fsub_rn(uv2.x, uv0.x), v));
-        float tvv = __fadd_rn(__fadd_rn(uv0.y, __fmul_rn(__fsub_rn(uv1.y, uv0.y), u)), __fmul_rn(__fsub_rn(uv2.y, uv0.y), v));
-        f3 tg = mk1(0.f), bt = mk1(0.f);
-        if (S.tri_t) {
-          const float4* tt = S.tri_t + 3 * (size_t)slot;
-          f3 g0 = from4(__ldg(tt)), g1 = from4(__ldg(tt + 1)), g2 = from4(__ldg(tt + 2));
-          tg = xadd(xadd(g0, xscale(xsub(g1, g0), u)), xscale(xsub(g2, g0), v));
-          bt = xscale(xcross(sn, tg), n0.w);
-        }
-        // kernel.cu:54-119 generateHitData
-        const DevMaterial& M = S.mats[__float_as_int(v2.w)];
-        HitData hd;
-        hd.albedo = M.albedo_tex < 0 ? mk(M.albedo[0], M.albedo[1], M.albedo[2]) : tex_uv(S, S.texs[M.albedo_tex], tu, tvv);
-        hd.emission = M.emission_tex < 0 ? mk(M.emission[0], M.emission[1], M.emission[2])
-                                         : tex_uv(S, S.texs[M.emission_tex], tu, tvv);
-        float rough = M.roughness_tex < 0 ? M.roughness : tex_uv(S, S.texs[M.roughness_tex], tu, tvv).x;
-        float metal = M.metallic_tex < 0 ? M.metallic : tex_uv(S, S.texs[M.metallic_tex], tu, tvv).x;
-        if (M.normal_tex < 0) {
-          hd.normal = sn;
-        } else {
-          f3 c = tex_uv(S, S.texs[M.normal_tex], tu, tvv);
-          f3 ln = c * 2.0f - mk1(1.0f);
-          hd.normal = normalized(tg * ln.x - bt * ln.y + sn * ln.z);
-        }
-        hd.roughness = powf(rough, 2.2f);
-        hd.metallic = powf(metal, 2.2f);
-        hd.clearcoatGloss = M.clearcoat_gloss;
-        hd.clearcoat = M.clearcoat;
-        hd.anisotropic = M.anisotropic;
-        hd.transmission = M.transmission;
-        hd.specular = M.specular;
-        hd.specularTint = M.specular_tint;
-        hd.sheenTint = M.sheen_tint;
-        hd.subsurface = M.subsurface;
-        hd.sheen = M.sheen;
-
         int32_t pix = local % P.npix, s = local / P.npix;
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
-        uint4 rn = philox(make_uint4(idx, (uint32_t)(P.sample_base + s), 2u + (uint32_t)bounce, 0u), P.k0, P.k1);
-        DisneyCtx C = disney_ctx(hd, d);
-        f3 dir = disney_sample(hd, C, u01(rn.x), u01(rn.y), u01(rn.z));
-        float r1 = u01(rn.w);
-        // shade, kernel.cu:339-358
-        f3 f = disney_eval(hd, C, dir);
-        float brdfPdf = disney_pdf(C, dir);
-        float ndl = fabsf(dot(dir, hd.normal));
-        // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked)
-        const DevTex& E = S.env;
-        int32_t cnt;
-        if ((P.flags & ER_RENDER_ENV_ALIAS) && S.alias_idx) {
-          // O(1) draw from the search's effective distribution (env.cu):
-          // column from the shared light word, coin from a second word
-          uint32_t coin = philox(make_uint4(idx, (uint32_t)(P.sample_base + s), 2u + (uint32_t)bounce, 1u), P.k0,
-                                 P.k1).x;
-          int32_t col = (int32_t)__umulhi(rn.w, (uint32_t)(E.w * E.h));
-          cnt = coin < __ldg(S.alias_thresh + col) ? col : __ldg(S.alias_idx + col);
-        } else {
-          cnt = hdri_search(S.cdf, r1, E.w * E.h);
-        }
-        float nu = __fdiv_rn((float)(cnt % E.w), (float)E.w), nv = __fdiv_rn((float)(cnt / E.w), (float)E.h);
-        int32_t ix = __float2int_rz(nu * (float)E.w), iy = __float2int_rz(nv * (float)E.h);
-        ix = __float2int_rz(E.x_tile * ((float)ix - E.x_offset * (float)E.w)) % E.w;
-        iy = __float2int_rz(E.y_tile * ((float)iy - E.y_offset * (float)E.h)) % E.h;
-        float iu = __fdiv_rn((float)ix, (float)E.w), iv = __fdiv_rn((float)iy, (float)E.h);
-        limit_uv(iu, iv);
-        f3 dH = -normalized(reverse_spherical(iu, iv));
-        float hdriPdf = hdri_pdf(S, __float2int_rz(iu * (float)E.w), __float2int_rz(iv * (float)E.h));
-        f3 eH = tex_uv(S, E, iu, iv);
-        f3 fH = disney_eval(hd, C, dH);
-        f3 hdriC = (fH * fabsf(dot(dH, hd.normal))) * eH / hdriPdf;
-        env_o = xadd(pos, xscale(dH, 0.001f));
-        env_d = xnormalize(dH);
+        VertexShade V;
+        shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
+        env_o = V.env_o;
+        env_d = V.env_d;
         push_env = true;
-        // point light NEE, kernel.cu:175-205
-        float pointPdf = 0.f;
-        f3 pointC = mk1(0.f);
-        if (S.n_lights > 0) {
-          pointPdf = (float)S.n_lights / (2.0f * ER_PI);
-          int32_t li = min(__float2int_rz((float)S.n_lights * r1), S.n_lights - 1);
-          const er_point_light& Lp = S.lights[li];
-          f3 lp = mk(Lp.position[0], Lp.position[1], Lp.position[2]);
-          f3 toL = xsub(lp, pos);
-          f3 dP = normalized(toL);
-          float dist = xlen(toL);
-          f3 fP = disney_eval(hd, C, dP);
-          f3 plv = mk(Lp.radiance[0], Lp.radiance[1], Lp.radiance[2]) / (dist * dist);
-          pointC = (plv * fP) * fabsf(dot(dP, hd.normal)) / pointPdf;
-          pt_o = xadd(pos, xscale(dP, 0.001f));
-          pt_d = xnormalize(dP);
-          pt_p = pos;
-          pt_dist = dist;
+        if (V.has_pt) {
+          pt_o = V.pt_o;
+          pt_d = V.pt_d;
+          pt_p = V.pos;
+          pt_dist = V.dist;
           push_pt = true;
         }
-        f3 brdfC = (f * ndl) * hd.emission / brdfPdf;
-        float den = hdriPdf + pointPdf + brdfPdf;
-        float w1 = hdriPdf / den, w2 = pointPdf / den, w3 = brdfPdf / den;
-        f3 tH = hdriC * w1, tP = pointC * w2, tB = brdfC * w3;
         uint32_t fl = 1u | (push_pt ? 2u : 0u);
-        w.pend[4 * (size_t)p] = make_float4(tH.x, tH.y, tH.z, w1 * 0.0f);
-        w.pend[4 * (size_t)p + 1] = make_float4(tP.x, tP.y, tP.z, w2 * 0.0f);
-        w.pend[4 * (size_t)p + 2] = make_float4(tB.x, tB.y, tB.z, __uint_as_float(fl));
+        w.pend[4 * (size_t)p] = make_float4(V.tH.x, V.tH.y, V.tH.z, V.w1 * 0.0f);
+        w.pend[4 * (size_t)p + 1] = make_float4(V.tP.x, V.tP.y, V.tP.z, V.w2 * 0.0f);
+        w.pend[4 * (size_t)p + 2] = make_float4(V.tB.x, V.tB.y, V.tB.z, __uint_as_float(fl));
         w.pend[4 * (size_t)p + 3] = make_float4(thr.x, thr.y, thr.z, 0.f);
-        f3 g = (f * ndl) / brdfPdf;
-        thr = mk(__fmul_rn(thr.x, g.x), __fmul_rn(thr.y, g.y), __fmul_rn(thr.z, g.z));
+        thr = mk(__fmul_rn(thr.x, V.g.x), __fmul_rn(thr.y, V.g.y), __fmul_rn(thr.z, V.g.z));
         w.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
         if (bounce == 0 && w.aov) {
-          w.aovs[3 * (size_t)p] = make_float4(sn.x, sn.y, sn.z, 0.f);
-          w.aovs[3 * (size_t)p + 1] = make_float4(tg.x, tg.y, tg.z, 0.f);
-          w.aovs[3 * (size_t)p + 2] = make_float4(bt.x, bt.y, bt.z, 0.f);
+          w.aovs[3 * (size_t)p] = make_float4(V.sn.x, V.sn.y, V.sn.z, 0.f);
+          w.aovs[3 * (size_t)p + 1] = make_float4(V.tg.x, V.tg.y, V.tg.z, 0.f);
+          w.aovs[3 * (size_t)p + 2] = make_float4(V.bt.x, V.bt.y, V.bt.z, 0.f);
         }
         if (!last) {
           // kernel.cu:442
-          next_o = xadd(pos, xscale(dir, 0.001f));
-          next_d = xnormalize(dir);
+          next_o = xadd(V.pos, xscale(V.dir, 0.001f));
+          next_d = xnormalize(V.dir);
           push_next = true;
         }
       }

@@ -121,6 +121,8 @@ er_status validate(const er_scene_desc* d) {
   return validate_texture(d->env, "environment");
 }
 
+}  // namespace
+
 // HDRI.hpp:107-128 through Texture::getValueFromCoordinates (Texture.hpp:95-
 // 112): FP32 running sums in row-major order.  Sequential on purpose: the
 // reference's rounding of the running sum is part of the sampled
@@ -150,6 +152,8 @@ void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum)
     for (int32_t i = 0; i < t.width; i++, c++) cdf[(size_t)c + 1] = cdf[(size_t)c] + texel(i, j) / sum;
   *radiance_sum = sum;
 }
+
+namespace {
 
 void pack_texels(const er_texture& t, std::vector<float4>& pool, DevTex* dt) {
   dt->w = t.width;
@@ -342,6 +346,9 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   I.max_shading_offset = br.max_delta;
   I.bvh_depth = br.depth;
   I.bvh_format = o.bvh_format;
+  I.material_count = d->material_count;
+  I.env_width = d->env.width;
+  I.env_height = d->env.height;
   I.device_bytes = s->device_bytes;
   *out = s;
   return ER_OK;

@@ -110,6 +110,8 @@ class er_scene_info(C.Structure):
         ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3),
         ("max_shading_offset", C.c_float),
         ("bvh_depth", C.c_int32), ("bvh_format", C.c_int32),
+        ("material_count", C.c_int32), ("env_width", C.c_int32), ("env_height", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -166,6 +168,7 @@ EXPORTED = [
     "er_scene_create", "er_scene_load", "er_scene_info_get",
     "er_scene_set_camera", "er_scene_get_camera", "er_scene_free",
     "er_render", "er_film_read", "er_render_paths", "er_render_noalloc", "er_env_distribution",
+    "er_scene_get_params", "er_scene_set_params", "er_render_replay", "er_backward",
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",
     "er_trace_closest", "er_encode_ldr", "er_write_image",

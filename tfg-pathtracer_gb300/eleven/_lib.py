@@ -67,6 +67,16 @@ def load(build_if_missing=True):
     L.er_render_noalloc.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_render_paths.restype = A.er_status
     L.er_render_paths.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p]
+    L.er_scene_get_params.restype = A.er_status
+    L.er_scene_get_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.er_scene_set_params.restype = A.er_status
+    L.er_scene_set_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]
+    L.er_render_replay.restype = A.er_status
+    L.er_render_replay.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]
+    L.er_backward.restype = A.er_status
+    L.er_backward.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.POINTER(A.er_render_stats)]
     L.er_batch_create.restype = A.er_status
     L.er_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(A.er_scene_opts),
                                   C.POINTER(C.c_void_p)]
@@ -186,6 +196,55 @@ class Scene:
                                _p(samples), _p(pc), C.byref(st)), "er_render")
         return dict(beauty=beauty, normal=aovs[0], tangent=aovs[1], bitangent=aovs[2], samples=samples,
                     pathcount=pc, stats=st)
+
+    # ---- differentiable parameters (host numpy arrays)
+    def env_hw(self):
+        """(h, w) of the environment texture."""
+        i = self.info()
+        return int(i.env_height), int(i.env_width)
+
+    def material_count(self):
+        return int(self.info().material_count)
+
+    def get_params(self):
+        """(materials (n, 5): albedo rgb, roughness, metallic; env (h, w, 3))."""
+        h, w = self.env_hw()
+        mats = np.zeros((self.material_count(), 5), np.float32)
+        env = np.zeros((h, w, 3), np.float32)
+        check(load().er_scene_get_params(self.h, _p(mats), _p(env)), "er_scene_get_params")
+        return mats, env
+
+    def set_params(self, materials=None, env=None):
+        m = None if materials is None else np.ascontiguousarray(materials, np.float32)
+        e = None if env is None else np.ascontiguousarray(env, np.float32)
+        check(load().er_scene_set_params(self.h, _p(m), _p(e), 0), "er_scene_set_params")
+
+    def render_replay(self, spp, max_depth=5, seed=0, sample_begin=0, materials=None, env=None, flags=0):
+        """Forward render by path replay; materials/env = evaluation
+        parameters (sampling stays with the scene's)."""
+        W, H = self.resolution
+        o = A.er_render_opts(spp, sample_begin, max_depth, 0, seed, flags, 0)
+        m = None if materials is None else np.ascontiguousarray(materials, np.float32)
+        e = None if env is None else np.ascontiguousarray(env, np.float32)
+        beauty = np.zeros((H * W, 4), np.float32)
+        samples = np.zeros(H * W, np.uint32)
+        pc = np.zeros(H * W, np.uint32)
+        check(load().er_render_replay(self.h, C.byref(o), _p(m), _p(e), _p(beauty), _p(samples), _p(pc)),
+              "er_render_replay")
+        return dict(beauty=beauty, samples=samples, pathcount=pc)
+
+    def backward(self, spp, d_beauty, samples, max_depth=5, seed=0, sample_begin=0, flags=0):
+        """Gradients (materials (n, 5), env (h, w, 3)) of a loss whose
+        derivative with respect to the film is d_beauty ((H*W, 4))."""
+        o = A.er_render_opts(spp, sample_begin, max_depth, 0, seed, flags, 0)
+        h, w = self.env_hw()
+        gm = np.zeros((self.material_count(), 5), np.float32)
+        ge = np.zeros((h, w, 3), np.float32)
+        db = np.ascontiguousarray(d_beauty, np.float32)
+        sa = np.ascontiguousarray(samples, np.uint32)
+        st = A.er_render_stats()
+        check(load().er_backward(self.h, C.byref(o), _p(db), _p(sa), _p(gm), _p(ge), C.byref(st)), "er_backward")
+        return gm, ge, st
 
     def render_paths(self, spp, max_depth=5, seed=0, sample_begin=0):
         W, H = self.resolution

@@ -522,6 +522,33 @@ def config2(n_jobs=64, seed=2, tri_lo=10_000, tri_hi=500_000, resolutions=C2_RES
     return arrays, jobs
 
 
+def config4(x_res=512, y_res=512, n_obj=64, geom_seed=4, param_seed=40, env_w=256, env_h=128, subdiv=3):
+    """Differentiation: n_obj icospheres placed as in the small scene (centres
+    U[-5,5]^3, radii U[0.3,1]), one point light, and a log-normal
+    env_w x env_h environment (n_obj * 5 + env_w * env_h * 3 parameters).  The differentiable parameters
+    (albedo U[0,1]^3, roughness U[0.05,1], metallic Bernoulli(0.3) per
+    object, env texels) are drawn from param_seed, so two param seeds give
+    a scene and a target with the same geometry."""
+    rng = np.random.default_rng(geom_seed)
+    prng = np.random.default_rng(param_seed)
+    base_v, base_f = icosphere(subdiv)
+    meshes, mats = [], []
+    for i in range(n_obj):
+        c = rng.uniform(-5, 5, 3)
+        r = rng.uniform(0.3, 1.0)
+        meshes.append((base_v * r + c, base_f, base_v.copy(), sphere_uv(base_v)))
+        mats.append(dict(albedo=tuple(prng.uniform(0, 1, 3)), roughness=prng.uniform(0.05, 1.0),
+                         metallic=float(prng.uniform() < 0.3), specular=0.5, clearcoat=0.0))
+    P, N, U, O = _assemble(meshes)
+    cam = dict(x_res=x_res, y_res=y_res, focal_length=pinhole_focal(45.0), position=(0.0, 1.0, -16.0),
+               rotation=(0.0, 0.0, 0.0), bokeh=False)
+    lights = np.array([[[0, 8, 0], [100, 100, 100]]], np.float32)
+    env = lognormal_env(env_w, env_h, param_seed, sigma=1.0, sun=0)
+    return SceneArrays(camera=cam, positions=P, normals=N, uvs=U, tri_object=O,
+                       object_material=np.arange(len(meshes), dtype=np.int32), materials=mats,
+                       lights=lights, env=env, name="c4")
+
+
 def random_rays(scene, n, seed=3):
     """Origins uniform in the scene bounds, directions uniform on the sphere
     (z = 1-2u, phi = 2 pi v)."""
