@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=128)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c1", "c0", "c2"])
+    ap.add_argument("--config", default="c1", choices=["c1", "c0", "c2", "c4"])
+    ap.add_argument("--fd-params", type=int, default=32, help="c4: parameters in the finite-difference check")
     ap.add_argument("--jobs", type=int, default=64, help="c2: number of batch jobs")
     ap.add_argument("--bvh", default="fp32", choices=["fp32", "q8"])
     ap.add_argument("--e2e-steps", type=int, default=16)
@@ -409,6 +410,101 @@ def run_batch(args):
     return 0
 
 
+def run_adjoint(args):
+    """c4: gradients of an L2 image loss with respect to 98,624 parameters
+    (64 objects x 5 Disney parameters + a 256x128 RGB environment), 512x512,
+    64 spp forward + 64 spp path-replay adjoint, max depth 6.  A step is one
+    forward render (er_render) plus one er_backward; value = full-gradient
+    evaluations per second.  The check: central differences (h = 1e-3,
+    common random numbers) of the detached estimator on --fd-params random
+    parameters, at 16 spp."""
+    from eleven import _lib, scenes
+    spp, depth = 64, 6
+    arrays = scenes.config4()
+    target = scenes.config4(param_seed=41)
+    s = _lib.Scene(arrays)
+    t = _lib.Scene(target)
+    T = t.render(spp, max_depth=depth, seed=99)["beauty"]
+    t.close()
+    m0, e0 = s.get_params()
+    n_params = m0.size + e0.size
+
+    def step(seed):
+        out = s.render(spp, max_depth=depth, seed=seed)
+        d = np.zeros_like(out["beauty"])
+        d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
+        gm, ge, st = s.backward(spp, d, out["samples"], max_depth=depth, seed=seed)
+        return out["stats"].ms, st.ms, gm, ge
+
+    for w in range(max(1, args.warmup)):
+        step(1000 + w)
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    res = [step(k) for k in range(args.steps)]
+    wall = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    fwd = float(np.median([r[0] for r in res]))
+    bwd = float(np.median([r[1] for r in res]))
+    # the replay walk alone (forward render by per-pixel replay, no gradients)
+    t0 = time.perf_counter()
+    s.render_replay(spp, max_depth=depth, seed=7)
+    replay_ms = (time.perf_counter() - t0) * 1e3
+
+    # finite-difference check of the detached estimator at 16 spp
+    fspp, h = 16, 1e-3
+    out = s.render(fspp, max_depth=depth, seed=5)
+    d = np.zeros_like(out["beauty"])
+    d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
+    gm, ge, _ = s.backward(fspp, d, out["samples"], max_depth=depth, seed=5)
+    g = np.concatenate([gm.ravel(), ge.ravel()])
+    rng = np.random.default_rng(32)
+    idx = rng.choice(n_params, args.fd_params, replace=False)
+
+    def loss(img):
+        dd = img[:, :3].astype(np.float64) - T[:, :3].astype(np.float64)
+        return float((dd * dd).sum())
+
+    gmax = float(np.abs(g).max())
+    errs, skipped = [], 0
+    for k in idx:
+        vals = []
+        for sign in (1, -1):
+            m, e = m0.copy(), e0.copy()
+            if k < m0.size:
+                m.ravel()[k] += sign * h
+            else:
+                e.ravel()[k - m0.size] += sign * h
+            vals.append(loss(s.render_replay(fspp, max_depth=depth, seed=5, materials=m, env=e)["beauty"]))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        if max(abs(fd), abs(g[k])) < 1e-4 * gmax:
+            skipped += 1
+            continue
+        errs.append(abs(fd - g[k]) / max(abs(fd), abs(g[k])))
+    s.close()
+    line = {
+        "metric": "adjoint full-gradient evaluations/s (512x512, 64 spp forward + 64 spp replay, depth 6)",
+        "value": round(1e3 / (fwd + bwd), 4), "unit": "grads/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(fwd + bwd, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, reference scene shapes)",
+        "config": {"workload": "c4: 64 icospheres (1280 tris each), 1 point light, 256x128 log-normal env; "
+                               "L2 loss to a render with other seeded parameters",
+                   "parameters": int(n_params), "spp": spp, "max_depth": depth},
+        "forward_ms": round(fwd, 2), "backward_ms": round(bwd, 2), "replay_forward_wall_ms": round(replay_ms, 1), "wall_ms_per_step": round(wall * 1e3, 2),
+        "backward_msamples_per_s": round(512 * 512 * spp / bwd / 1e3, 2),
+        "fd_check": {"params": int(args.fd_params), "checked": len(errs), "negligible": skipped,
+                     "max_rel_err": round(float(max(errs)) if errs else 0.0, 6),
+                     "median_rel_err": round(float(np.median(errs)) if errs else 0.0, 6),
+                     "h": h, "spp": fspp, "estimator": "detached sampling (er_render_replay)"},
+        "gpu_launches": 2,
+    }
+    if clk:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def launch_rays(args):
     """Rays in trace launch b of a 1-spp wave at sample index 1 (the first
     warm-up step of the default run): extension rays of bounce b plus shadow
@@ -443,6 +539,8 @@ def main():
         return run_reference(args)
     if args.config == "c2":
         return run_batch(args)
+    if args.config == "c4":
+        return run_adjoint(args)
     return run_gpu(args)
 
 

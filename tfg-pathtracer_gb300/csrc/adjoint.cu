@@ -12,14 +12,16 @@
 // value (continuation, env and light directions) and every environment
 // radiance (escape and next-event texel).
 //
-// One thread owns one pixel and walks its samples in order.  Per sample it
-// re-traces the path from its counter-based random numbers twice: once for
-// the sample's radiance L (which sets the clamp mask and the NaN drop of the
-// accumulation, kernel.cu:445-449), once to scatter gradients.  At vertex i
-// the replay knows the throughput beta_i, the radiance L_<=i gathered so far
-// and therefore the radiance still to come, L - L_<=i, which carries vertex
-// i's throughput factor f_i |N.L| / pdf_i: its derivative is
-// (L - L_<=i) * df_i / f_i per channel.  Nothing per vertex is stored.
+// Backward: the wavefront forward first gives every sample's radiance L
+// (12 bytes per path; it sets the clamp mask and the NaN drop of the
+// accumulation, kernel.cu:445-449).  Then one thread per path re-traces the
+// path from its counter-based random numbers and scatters gradients.  At
+// vertex i the replay knows the throughput beta_i, the radiance L_<=i
+// gathered so far and therefore the radiance still to come, L - L_<=i,
+// which carries vertex i's throughput factor f_i |N.L| / pdf_i: its
+// derivative is (L - L_<=i) * df_i / f_i per channel.  Nothing per vertex is
+// stored.  Material gradients collect in shared memory per block of the
+// persistent grid, env gradients with global atomics.
 //
 // The same walk without gradients is a complete forward render
 // (er_render_replay): with the evaluation parameters equal to the scene's
@@ -37,8 +39,10 @@ namespace er {
 namespace {
 
 // ---------------------------------------------------------------- duals --
-// Forward-mode dual number over the 5 material parameters of one vertex.
-constexpr int kNP = 5;
+// Forward-mode dual number carrying the derivative along one material
+// parameter (the replay loops over the kParams parameters of a vertex).
+constexpr int kNP = 1;
+constexpr int kParams = 5;  // albedo r, g, b, roughness, metallic
 
 struct Dual {
   float v;
@@ -190,36 +194,70 @@ struct ReplayArgs {
 };
 
 template <int MODE, bool Q8>
-__device__ __forceinline__ void trace_one(const DevScene& S, Traverser<MODE, Q8, false>& tr, int2* sstk,
-                                          uint32_t* err) {
+__device__ __forceinline__ void trace_warp(const DevScene& S, Traverser<MODE, Q8, false>& tr, int2* sstk,
+                                          bool active, uint32_t* err) {
+  // Called by all 32 lanes together; lanes without a ray pass active =
+  // false.  Node and leaf rounds are chosen by warp vote as in the
+  // persistent traversal, so the lanes stay converged.  Every node is
+  // expanded and every leaf tested at most once per ray: the walk is
+  // bounded by a multiple of the node count.
   int2 lstk[kLocalStack];
   TravStats st{0, 0, 0};
-  // every node is expanded at most once and every leaf tested at most once
-  // per ray, so the walk is bounded by twice the node count
-  for (int64_t it = 0; !tr.done; it++) {
-    if (tr.leaf != 0) tr.leaf_step(S, sstk, lstk, st, err);
-    else if (tr.node >= 0) tr.node_step(S, sstk, lstk, st, err);
-    else tr.finish();
-    if (it > 8 * S.n_nodes + 64) {
-      atomicOr(err, 4u);
-      tr.done = true;
+  bool busy = active && !tr.done;
+  const int64_t lim = 8 * S.n_nodes + 64;
+  int64_t it = 0;
+  while (__any_sync(0xFFFFFFFFu, busy)) {
+    const bool node_only = busy && tr.node >= 0 && tr.leaf == 0;
+    const bool leaf_round = !__any_sync(0xFFFFFFFFu, node_only);
+    if (busy) {
+      if (leaf_round) {
+        if (tr.leaf != 0) tr.leaf_step(S, sstk, lstk, st, err);
+        else if (tr.node < 0) tr.finish();
+      } else if (tr.node >= 0) {
+        tr.node_step(S, sstk, lstk, st, err);
+      }
+      if (++it > lim) {
+        atomicOr(err, 4u);
+        tr.done = true;
+      }
+      busy = !tr.done;
     }
   }
 }
 
-// Adds v to gradient slot i (shared-memory copy when it fits).
-__device__ __forceinline__ void add_mat(const ReplayArgs& A, float* sg, int32_t i, float v) {
-  if (v == 0.f || !(fabsf(v) < INFINITY)) return;
-  if (A.smem_grad) atomicAdd(&sg[i], v);
-  else atomicAdd(&A.g_mat[i], v);
+// base[key * N + k] += v[k], warp-aggregated: the converged lanes that
+// share a key (neighbouring pixels see the same env texel and object) are
+// summed with shuffles and one lane issues the N atomics.  Non-finite
+// contributions are dropped.
+template <int N>
+__device__ __forceinline__ void agg_add(float* base, int64_t key, float (&v)[N]) {
+#pragma unroll
+  for (int k = 0; k < N; k++)
+    if (!(fabsf(v[k]) < INFINITY)) v[k] = 0.f;
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, (unsigned long long)key);
+  float s[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) s[k] = 0.f;
+  for (unsigned m = peers; m; m &= m - 1) {
+    const int src = __ffs(m) - 1;
+#pragma unroll
+    for (int k = 0; k < N; k++) s[k] += __shfl_sync(peers, v[k], src);
+  }
+  if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
+#pragma unroll
+    for (int k = 0; k < N; k++)
+      if (s[k] != 0.f) atomicAdd(&base[key * N + k], s[k]);
+  }
 }
 
-// One sample of pixel (x, y).  GRAD = false: returns the sample's radiance
-// and vertex count.  GRAD = true: the replay, given the sample's radiance
-// Lt and its adjoint dl (d loss / d radiance).
+// One sample of pixel (x, y), called by all 32 lanes of the warp together
+// (active = false: a lane without a path this round).  GRAD = false:
+// returns the sample's radiance and vertex count.  GRAD = true: the replay,
+// given the sample's radiance Lt and its adjoint dl (d loss / d radiance).
 template <bool Q8, bool GRAD, bool EVAL>
-__device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg, int32_t x, int32_t y, uint32_t idx,
-                   uint32_t sample, f3 Lt, f3 dl, int32_t* bounces) {
+__device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg, bool active, int32_t x, int32_t y,
+                   uint32_t idx, uint32_t sample, f3 Lt, f3 dl, int32_t* bounces) {
   const WaveParams& P = A.P;
   uint4 ra = philox(make_uint4(idx, sample, 0u, 0u), P.k0, P.k1);
   uint4 rb = philox(make_uint4(idx, sample, 1u, 0u), P.k0, P.k1);
@@ -228,11 +266,23 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
   f3 thr = mk1(1.0f);
   float Lx = 0.f, Ly = 0.f, Lz = 0.f;
   *bounces = P.max_depth;
+  bool alive = active;
   for (int32_t bounce = 0; bounce < P.max_depth; bounce++) {
-    Traverser<kClosest, Q8, false> tr;
-    tr.init(S, o, d, mk1(0.f), 0.f);
-    trace_one(S, tr, sstk, A.err);
-    if (tr.slot < 0) {
+    if (!__any_sync(0xFFFFFFFFu, alive)) break;
+    int32_t hslot = -1;
+    float ht = 0.f, hu = 0.f, hv = 0.f;
+    {
+      Traverser<kClosest, Q8, false> tr;
+      if (alive) tr.init(S, o, d, mk1(0.f), 0.f);
+      trace_warp(S, tr, sstk, alive, A.err);
+      if (alive) {
+        hslot = tr.slot;
+        ht = tr.t;
+        hu = tr.u;
+        hv = tr.v;
+      }
+    }
+    if (alive && hslot < 0) {
       // kernel.cu:414-419
       int64_t te;
       f3 e = escape_radiance(S, d, &te);
@@ -241,26 +291,46 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
       Ly = __fadd_rn(Ly, __fmul_rn(e.y, thr.y));
       Lz = __fadd_rn(Lz, __fmul_rn(e.z, thr.z));
       if (GRAD) {
-        atomicAdd(&A.g_env[3 * te], dl.x * thr.x);
-        atomicAdd(&A.g_env[3 * te + 1], dl.y * thr.y);
-        atomicAdd(&A.g_env[3 * te + 2], dl.z * thr.z);
+        float ge[3] = {dl.x * thr.x, dl.y * thr.y, dl.z * thr.z};
+        agg_add<3>(A.g_env, te, ge);
       }
       *bounces = bounce;
-      break;
+      alive = false;
     }
+    // The vertex is shaded twice: once for its shadow rays, and again after
+    // tracing them (same inputs, same result), so that the shading state
+    // does not stay live across the traversals.
+    bool vH = false, vP = true, pt = false;
+    {
+      f3 eo = mk1(0.f), ed = mk1(0.f), po = mk1(0.f), pd = mk1(0.f), pp = mk1(0.f);
+      float pdist = 0.f;
+      if (alive) {
+        VertexShade V0;
+        shade_vertex(S, P.flags, P.k0, P.k1, idx, sample, bounce, o, d, ht, hu, hv, hslot, V0);
+        eo = V0.env_o;
+        ed = V0.env_d;
+        pt = V0.has_pt;
+        po = V0.pt_o;
+        pd = V0.pt_d;
+        pp = V0.pos;
+        pdist = V0.dist;
+      }
+      {
+        Traverser<kAny, Q8, false> te;
+        if (alive) te.init(S, eo, ed, mk1(0.f), 0.f);
+        trace_warp(S, te, sstk, alive, A.err);
+        vH = alive && !te.occluded;
+      }
+      {
+        Traverser<kPoint, Q8, false> tp;
+        if (pt) tp.init(S, po, pd, pp, pdist);
+        trace_warp(S, tp, sstk, pt, A.err);
+        if (pt) vP = !tp.occluded;
+      }
+    }
+    if (!alive) continue;
     VertexShade V;
-    shade_vertex(S, P.flags, P.k0, P.k1, idx, sample, bounce, o, d, tr.t, tr.u, tr.v, tr.slot, V);
-    Traverser<kAny, Q8, false> te;
-    te.init(S, V.env_o, V.env_d, mk1(0.f), 0.f);
-    trace_one(S, te, sstk, A.err);
-    const bool vH = !te.occluded;
-    bool vP = true;
-    if (V.has_pt) {
-      Traverser<kPoint, Q8, false> tp;
-      tp.init(S, V.pt_o, V.pt_d, V.pos, V.dist);
-      trace_one(S, tp, sstk, A.err);
-      vP = !tp.occluded;
-    }
+    shade_vertex(S, P.flags, P.k0, P.k1, idx, sample, bounce, o, d, ht, hu, hv, hslot, V);
     f3 tH = V.tH, tP = V.tP, tB = V.tB, g = V.g, f = V.f, fH = V.fH, fP = V.fP, eH = V.eH;
     const DevMaterial& M = S.mats[V.mat];
     if (EVAL) {
@@ -299,51 +369,49 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
     Ly = __fadd_rn(Ly, __fmul_rn(__fadd_rn(__fadd_rn(hy, py), tB.y), thr.y));
     Lz = __fadd_rn(Lz, __fmul_rn(__fadd_rn(__fadd_rn(hz, pz), tB.z), thr.z));
     if (GRAD) {
-      // d C_i: BRDF values of the three strategies, env texel of the NEE
+      // d C_i: BRDF values of the three strategies, env texel of the NEE.
+      // One parameter at a time (single-partial duals keep registers low).
       const bool ca = M.albedo_tex < 0, cr = M.roughness_tex < 0, cm = M.metallic_tex < 0;
-      D3 alb = d3c(0.f);
-      alb.x = dconst(V.hd.albedo.x);
-      alb.y = dconst(V.hd.albedo.y);
-      alb.z = dconst(V.hd.albedo.z);
-      if (ca) { alb.x.d[0] = 1.f; alb.y.d[1] = 1.f; alb.z.d[2] = 1.f; }
-      Dual rg = dconst(V.hd.roughness), mt = dconst(V.hd.metallic);
-      if (cr && V.rough_in > 0.f) rg.d[3] = 2.2f * powf(V.rough_in, 1.2f);
-      if (cm && V.metal_in > 0.f) mt.d[4] = 2.2f * powf(V.metal_in, 1.2f);
       const DisneyCtx& C = V.C;
-      D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
-      D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
       // strategy weights per channel: C_c = thr_c * (kH_c fH_c + kP_c fP_c + kB_c f_c)
-      f3 kH = vH ? eH * (V.cosH / V.hdriPdf * V.w1) : mk1(0.f);
-      f3 kB = V.hd.emission * (V.ndl / V.brdfPdf * V.w3);
-      f3 wd = mk(dl.x * thr.x, dl.y * thr.y, dl.z * thr.z);
-      float gk[kNP];
-#pragma unroll
-      for (int k = 0; k < kNP; k++)
-        gk[k] = wd.x * (kH.x * DfH.x.d[k] + kB.x * Df.x.d[k]) + wd.y * (kH.y * DfH.y.d[k] + kB.y * Df.y.d[k]) +
-                wd.z * (kH.z * DfH.z.d[k] + kB.z * Df.z.d[k]);
-      if (V.has_pt && vP) {
-        D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
-        f3 kP = V.plv * (V.cosP / V.pointPdf * V.w2);
-#pragma unroll
-        for (int k = 0; k < kNP; k++)
-          gk[k] += wd.x * kP.x * DfP.x.d[k] + wd.y * kP.y * DfP.y.d[k] + wd.z * kP.z * DfP.z.d[k];
-      }
+      const f3 kH = vH ? eH * (V.cosH / V.hdriPdf * V.w1) : mk1(0.f);
+      const f3 kB = V.hd.emission * (V.ndl / V.brdfPdf * V.w3);
+      const f3 kP = (V.has_pt && vP) ? V.plv * (V.cosP / V.pointPdf * V.w2) : mk1(0.f);
+      const f3 wd = mk(dl.x * thr.x, dl.y * thr.y, dl.z * thr.z);
       // radiance still to come carries f_i through the throughput
-      f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
-      f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
-                 f.z != 0.f ? dl.z * La.z / f.z : 0.f);
-#pragma unroll
-      for (int k = 0; k < kNP; k++) {
-        gk[k] += ra.x * Df.x.d[k] + ra.y * Df.y.d[k] + ra.z * Df.z.d[k];
-        add_mat(A, sg, 5 * V.mat + k, gk[k]);
+      const f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
+      const f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
+                       f.z != 0.f ? dl.z * La.z / f.z : 0.f);
+      float gk[kParams];
+#pragma unroll 1
+      for (int k = 0; k < kParams; k++) {
+        D3 alb{dconst(V.hd.albedo.x), dconst(V.hd.albedo.y), dconst(V.hd.albedo.z)};
+        Dual rg = dconst(V.hd.roughness), mt = dconst(V.hd.metallic);
+        bool seeded = false;
+        if (k == 0 && ca) { alb.x.d[0] = 1.f; seeded = true; }
+        if (k == 1 && ca) { alb.y.d[0] = 1.f; seeded = true; }
+        if (k == 2 && ca) { alb.z.d[0] = 1.f; seeded = true; }
+        if (k == 3 && cr && V.rough_in > 0.f) { rg.d[0] = 2.2f * powf(V.rough_in, 1.2f); seeded = true; }
+        if (k == 4 && cm && V.metal_in > 0.f) { mt.d[0] = 2.2f * powf(V.metal_in, 1.2f); seeded = true; }
+        float acc = 0.f;
+        if (seeded) {
+          D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
+          D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
+          acc = wd.x * (kH.x * DfH.x.d[0] + kB.x * Df.x.d[0]) + wd.y * (kH.y * DfH.y.d[0] + kB.y * Df.y.d[0]) +
+                wd.z * (kH.z * DfH.z.d[0] + kB.z * Df.z.d[0]) + ra.x * Df.x.d[0] + ra.y * Df.y.d[0] +
+                ra.z * Df.z.d[0];
+          if (V.has_pt && vP) {
+            D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
+            acc += wd.x * kP.x * DfP.x.d[0] + wd.y * kP.y * DfP.y.d[0] + wd.z * kP.z * DfP.z.d[0];
+          }
+        }
+        gk[k] = acc;
       }
+      agg_add<kParams>(A.smem_grad ? sg : A.g_mat, V.mat, gk);
       if (vH) {
         float s = V.cosH / V.hdriPdf * V.w1;
-        int64_t t3 = 3 * V.env_texel;
-        float a0 = wd.x * fH.x * s, a1 = wd.y * fH.y * s, a2 = wd.z * fH.z * s;
-        if (a0 != 0.f && fabsf(a0) < INFINITY) atomicAdd(&A.g_env[t3], a0);
-        if (a1 != 0.f && fabsf(a1) < INFINITY) atomicAdd(&A.g_env[t3 + 1], a1);
-        if (a2 != 0.f && fabsf(a2) < INFINITY) atomicAdd(&A.g_env[t3 + 2], a2);
+        float ge[3] = {wd.x * fH.x * s, wd.y * fH.y * s, wd.z * fH.z * s};
+        agg_add<3>(A.g_env, V.env_texel, ge);
       }
     }
     thr = mk(__fmul_rn(thr.x, g.x), __fmul_rn(thr.y, g.y), __fmul_rn(thr.z, g.z));
@@ -355,63 +423,92 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
   return mk(Lx, Ly, Lz);
 }
 
-template <bool Q8, bool GRAD, bool EVAL>
+// Forward render by replay: one thread per pixel, samples in order, with
+// accumulate_pixel's arithmetic.  Lanes past the image take part in the
+// warp's traversals without a path.
+template <bool Q8, bool EVAL>
 __global__ void __launch_bounds__(kTravBlock) k_replay(DevScene S, ReplayArgs A) {
+  __shared__ int2 stk[kSmemStack * kTravBlock];
+  const WaveParams& P = A.P;
+  const int32_t pix0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = pix0 < P.npix;
+  const int32_t pix = valid ? pix0 : 0;
+  const int32_t x = pix % P.W, y = pix / P.W;
+  const uint32_t idx = (uint32_t)(P.W * (P.H - y - 1) + x);  // kernel.cu:378
+  uint32_t sa = 0, pc = 0;
+  float4 bt = make_float4(0.f, 0.f, 0.f, 1.f);
+  for (int32_t s = 0; s < P.spp_wave; s++) {
+    int32_t nb;
+    f3 L = walk<Q8, false, EVAL>(S, A, stk + threadIdx.x, nullptr, valid, x, y, idx, (uint32_t)(P.sample_base + s),
+                                 mk1(0.f), mk1(0.f), &nb);
+    if (!valid) continue;
+    pc += (uint32_t)nb;
+    float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
+    if (isnan(lx) || isnan(ly) || isnan(lz)) continue;
+    float inv = __fadd_rn((float)sa, 1.0f);
+    if (sa > 0) {
+      float k = __fdiv_rn((float)sa, (float)(sa + 1));
+      bt.x = __fmul_rn(bt.x, k); bt.y = __fmul_rn(bt.y, k); bt.z = __fmul_rn(bt.z, k);
+    }
+    bt.x = __fadd_rn(bt.x, __fdiv_rn(lx, inv));
+    bt.y = __fadd_rn(bt.y, __fdiv_rn(ly, inv));
+    bt.z = __fadd_rn(bt.z, __fdiv_rn(lz, inv));
+    sa++;
+  }
+  if (!valid) return;
+  A.beauty[idx] = bt;
+  A.samples[idx] = sa;
+  A.pathcount[idx] = pc;
+}
+
+#ifndef ER_BWD_MIN_BLOCKS
+#define ER_BWD_MIN_BLOCKS 2
+#endif
+// Resident blocks of 128 per SM the register budget of k_backward allows.
+constexpr int kBackwardMinBlocks = ER_BWD_MIN_BLOCKS;
+
+// Gradient replay: one path per lane over a persistent grid; each warp
+// takes 32 consecutive paths (sample-major, so neighbouring lanes trace
+// neighbouring pixels).  The sample's radiance comes from the wavefront
+// forward's per-path dump.
+template <bool Q8>
+__global__ void __launch_bounds__(kTravBlock, kBackwardMinBlocks) k_backward(DevScene S, ReplayArgs A, const float* __restrict__ rad) {
   __shared__ int2 stk[kSmemStack * kTravBlock];
   extern __shared__ float sg[];
   const WaveParams& P = A.P;
-  if (GRAD && A.smem_grad) {
+  if (A.smem_grad) {
     for (int32_t i = threadIdx.x; i < 5 * A.n_mats; i += blockDim.x) sg[i] = 0.f;
     __syncthreads();
   }
-  const int32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix < P.npix) {
+  const int64_t N = (int64_t)P.npix * P.spp_wave;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int32_t lane = (int32_t)(threadIdx.x & 31u);
+  for (int64_t base = warp * 32; base < N; base += nwarps * 32) {
+    const int64_t q = base + lane;
+    bool act = q < N;
+    const int32_t pix = act ? (int32_t)(q % P.npix) : 0, s = act ? (int32_t)(q / P.npix) : 0;
     const int32_t x = pix % P.W, y = pix / P.W;
     const uint32_t idx = (uint32_t)(P.W * (P.H - y - 1) + x);  // kernel.cu:378
-    if (!GRAD) {
-      // forward render with accumulate_pixel's arithmetic
-      uint32_t sa = 0, pc = 0;
-      float4 bt = make_float4(0.f, 0.f, 0.f, 1.f);
-      for (int32_t s = 0; s < P.spp_wave; s++) {
-        int32_t nb;
-        f3 L = walk<Q8, false, EVAL>(S, A, stk + threadIdx.x, sg, x, y, idx, (uint32_t)(P.sample_base + s),
-                                     mk1(0.f), mk1(0.f), &nb);
-        pc += (uint32_t)nb;
-        float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
-        if (isnan(lx) || isnan(ly) || isnan(lz)) continue;
-        float inv = __fadd_rn((float)sa, 1.0f);
-        if (sa > 0) {
-          float k = __fdiv_rn((float)sa, (float)(sa + 1));
-          bt.x = __fmul_rn(bt.x, k); bt.y = __fmul_rn(bt.y, k); bt.z = __fmul_rn(bt.z, k);
-        }
-        bt.x = __fadd_rn(bt.x, __fdiv_rn(lx, inv));
-        bt.y = __fadd_rn(bt.y, __fdiv_rn(ly, inv));
-        bt.z = __fadd_rn(bt.z, __fdiv_rn(lz, inv));
-        sa++;
-      }
-      A.beauty[idx] = bt;
-      A.samples[idx] = sa;
-      A.pathcount[idx] = pc;
-    } else {
+    f3 L = mk1(0.f), dl = mk1(0.f);
+    if (act) {
       const uint32_t n = A.nvalid[idx];
       const float4 g4 = A.d_beauty[idx];
-      if (n > 0 && (g4.x != 0.f || g4.y != 0.f || g4.z != 0.f)) {
-        const float inv_n = 1.0f / (float)n;
-        for (int32_t s = 0; s < P.spp_wave; s++) {
-          int32_t nb;
-          const uint32_t sample = (uint32_t)(P.sample_base + s);
-          f3 L = walk<Q8, false, false>(S, A, stk + threadIdx.x, sg, x, y, idx, sample, mk1(0.f), mk1(0.f), &nb);
-          if (isnan(L.x) || isnan(L.y) || isnan(L.z)) continue;  // dropped by the accumulation
-          // clamp(L, 0, 10) passes the derivative only strictly inside
-          f3 dl = mk((L.x > 0.f && L.x < 10.f) ? g4.x * inv_n : 0.f, (L.y > 0.f && L.y < 10.f) ? g4.y * inv_n : 0.f,
-                     (L.z > 0.f && L.z < 10.f) ? g4.z * inv_n : 0.f);
-          if (dl.x == 0.f && dl.y == 0.f && dl.z == 0.f) continue;
-          walk<Q8, true, false>(S, A, stk + threadIdx.x, sg, x, y, idx, sample, L, dl, &nb);
-        }
-      }
+      const float* r = rad + 3 * ((int64_t)s * P.npix + idx);
+      L = mk(r[0], r[1], r[2]);
+      // dropped samples (NaN) get no gradient; clamp(L, 0, 10) passes the
+      // derivative only strictly inside
+      const float inv_n = n > 0 ? 1.0f / (float)n : 0.f;
+      const bool keep = n > 0 && !isnan(L.x) && !isnan(L.y) && !isnan(L.z);
+      dl = mk((keep && L.x > 0.f && L.x < 10.f) ? g4.x * inv_n : 0.f,
+              (keep && L.y > 0.f && L.y < 10.f) ? g4.y * inv_n : 0.f,
+              (keep && L.z > 0.f && L.z < 10.f) ? g4.z * inv_n : 0.f);
+      act = dl.x != 0.f || dl.y != 0.f || dl.z != 0.f;
     }
+    int32_t nb;
+    walk<Q8, true, false>(S, A, stk + threadIdx.x, sg, act, x, y, idx, (uint32_t)(P.sample_base + s), L, dl, &nb);
   }
-  if (GRAD && A.smem_grad) {
+  if (A.smem_grad) {
     __syncthreads();
     for (int32_t i = threadIdx.x; i < 5 * A.n_mats; i += blockDim.x)
       if (sg[i] != 0.f) atomicAdd(&A.g_mat[i], sg[i]);
@@ -420,13 +517,26 @@ __global__ void __launch_bounds__(kTravBlock) k_replay(DevScene S, ReplayArgs A)
 
 constexpr int kMaxSmemGrad = 8192;  // floats of shared memory for material gradients
 
-template <bool GRAD, bool EVAL>
+template <bool EVAL>
 er_status launch_replay(er_scene* s, const ReplayArgs& A) {
   const int32_t npix = A.P.npix;
   const unsigned blocks = (unsigned)((npix + kTravBlock - 1) / kTravBlock);
-  const size_t smem = (GRAD && A.smem_grad) ? (size_t)5 * A.n_mats * sizeof(float) : 0;
-  if (s->dev.use_q8) k_replay<true, GRAD, EVAL><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A);
-  else k_replay<false, GRAD, EVAL><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A);
+  if (s->dev.use_q8) k_replay<true, EVAL><<<blocks, kTravBlock, 0, s->stream>>>(s->dev, A);
+  else k_replay<false, EVAL><<<blocks, kTravBlock, 0, s->stream>>>(s->dev, A);
+  ER_CUDA(cudaGetLastError());
+  return ER_OK;
+}
+
+er_status launch_backward(er_scene* s, const ReplayArgs& A, const float* rad) {
+  const size_t smem = A.smem_grad ? (size_t)5 * A.n_mats * sizeof(float) : 0;
+  int occ = 0;
+  if (s->dev.use_q8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_backward<true>, kTravBlock, smem);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_backward<false>, kTravBlock, smem);
+  const int64_t N = (int64_t)A.P.npix * A.P.spp_wave;
+  const int64_t want = (N + kTravBlock - 1) / kTravBlock;
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(1, occ) * s->num_sms));
+  if (s->dev.use_q8) k_backward<true><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A, rad);
+  else k_backward<false><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A, rad);
   ER_CUDA(cudaGetLastError());
   return ER_OK;
 }
@@ -610,7 +720,7 @@ extern "C" er_status er_render_replay(er_scene* s, const er_render_opts* o, cons
     if ((st = T.alloc((void**)&A.pathcount, np * 4)) != ER_OK) return st;
   }
   if (np > 0) {
-    st = (em || ee) ? launch_replay<false, true>(s, A) : launch_replay<false, false>(s, A);
+    st = (em || ee) ? launch_replay<true>(s, A) : launch_replay<false>(s, A);
     if (st != ER_OK) return st;
   }
   if (!dev) {
@@ -650,8 +760,19 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
   else if ((st = T.alloc((void**)&A.g_env, env_n * 4)) != ER_OK) return st;
   ER_CUDA(cudaMemsetAsync(A.g_mat, 0, mat_n * 4, s->stream));
   ER_CUDA(cudaMemsetAsync(A.g_env, 0, env_n * 4, s->stream));
+  // the samples' radiance: the wavefront forward, one wave, per-path dump
+  const int64_t npaths = (int64_t)np * A.P.spp_wave;
+  float* d_rad = nullptr;
+  int32_t* d_b = nullptr;
+  if ((st = T.alloc((void**)&d_rad, (size_t)npaths * 12)) != ER_OK) return st;
+  if ((st = T.alloc((void**)&d_b, (size_t)npaths * 4)) != ER_OK) return st;
   ER_CUDA(cudaEventRecord(s->ev0, s->stream));
-  if (np > 0 && (st = launch_replay<true, false>(s, A)) != ER_OK) return st;
+  if (npaths > 0) {
+    er_render_opts oo = *o;
+    oo.flags &= ER_RENDER_ENV_ALIAS;
+    if ((st = render_paths_device(s, &oo, d_rad, d_b)) != ER_OK) return st;
+    if ((st = launch_backward(s, A, d_rad)) != ER_OK) return st;
+  }
   ER_CUDA(cudaEventRecord(s->ev1, s->stream));
   if (!dev) {
     if (grad_materials)
@@ -670,7 +791,7 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     stats->ms = ms;
     stats->samples = (int64_t)o->spp * (int64_t)np;
-    stats->kernel_launches = np > 0 ? 1 : 0;
+    stats->kernel_launches = npaths > 0 ? 2 * A.P.max_depth + 4 : 0;
   }
   return ER_OK;
 }

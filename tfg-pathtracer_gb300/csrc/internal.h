@@ -226,6 +226,10 @@ er_status build_env_alias(er_scene* s);
 // Environment CDF and radiance sum as the reference builds them (scene.cpp).
 void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum);
 
+// Per-path radiance (spp x npix x 3, sample-major, output index order) and
+// vertex counts of the samples er_render makes with opts, into device
+// buffers, in one wave (render.cu).
+er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b);
 // Wavefront buffers for `cap` paths (render.cu); stats = device ray counters.
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out);
 void wave_destroy(Wave* w);

@@ -679,6 +679,12 @@ void free_film(er_scene* s) {
   F = Film();
 }
 
+er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b) {
+  er_render_opts oo = *o;
+  oo.flags &= ~(uint32_t)ER_RENDER_AOV;
+  return run(s, &oo, d_rad, d_b, nullptr);
+}
+
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out) {
   Wave* ww = new Wave();
   er_status st = wave_fill(ww, cap, false, stats);
