@@ -142,6 +142,14 @@ void orc_render(const orc_scene* s, const orc_render_opts* o, float* beauty, flo
  * radiance [s][p][3], bounces [s][p], p = output pixel index. */
 void orc_render_paths(const orc_scene* s, const orc_render_opts* o, float* radiance, int32_t* bounces);
 
+/* ---- FP64 restatement of the estimator (orc64.c) ---- */
+typedef struct orc64_scene orc64_scene;
+orc64_scene* orc64_new(const orc_scene* s);
+void orc64_free(orc64_scene* S);
+void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
+                         int32_t max_depth, uint64_t seed, double* rgb, uint32_t* counts, int32_t nthreads);
+void orc64_trace(const orc64_scene* S, const float* rays, int64_t n, int32_t* tri, double* dist, int32_t nthreads);
+
 /* ---- output (main.cpp:150-165) ---- */
 double orc_fastpow(double a, double b);
 void orc_encode_ldr(const float* rgba, int64_t n, uint8_t* out);

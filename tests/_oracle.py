@@ -51,6 +51,12 @@ def orc():
         _orc.orc_p_sample_u.argtypes = [C.c_void_p, C.c_int64, A.IP, C.c_int32, A.FP, A.FP]
         _orc.orc_p_philox.argtypes = [C.c_int64, A.UP, C.c_uint32, C.c_uint32, A.UP]
         _orc.orc_p_hdri_counts.argtypes = [A.FP, C.c_int32, A.UP]
+        _orc.orc64_new.restype = C.c_void_p
+        _orc.orc64_new.argtypes = [C.c_void_p]
+        _orc.orc64_free.argtypes = [C.c_void_p]
+        _orc.orc64_render_pixels.argtypes = [C.c_void_p, A.IP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                             C.c_uint64, C.POINTER(C.c_double), A.UP, C.c_int32]
+        _orc.orc64_trace.argtypes = [C.c_void_p, A.FP, C.c_int64, A.IP, C.POINTER(C.c_double), C.c_int32]
     return _orc
 
 
@@ -158,6 +164,40 @@ def texture(img, offset=(0.0, 0.0), tile=(1.0, 1.0)):
     keep = []
     fill_texture(t, img, keep, offset=offset, tile=tile)
     return t, keep
+
+
+class Orc64:
+    """FP64 restatement of the estimator over an OrcScene (own BVH)."""
+
+    def __init__(self, orc_scene):
+        self.base = orc_scene
+        self.h = orc().orc64_new(orc_scene.h)
+
+    def close(self):
+        if self.h:
+            orc().orc64_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def render_pixels(self, idx, spp, max_depth, seed=0, sample_begin=0, nthreads=0):
+        """Mean of clamp(L, 0, 10) over non-NaN samples for the pixels with
+        output indices idx: (rgb (n, 3) float64, counts (n,))."""
+        idx = np.ascontiguousarray(idx, np.int32)
+        rgb = np.zeros((len(idx), 3), np.float64)
+        cnt = np.zeros(len(idx), np.uint32)
+        orc().orc64_render_pixels(self.h, _ptr(idx, A.IP), len(idx), spp, sample_begin, max_depth, seed,
+                                  rgb.ctypes.data_as(C.POINTER(C.c_double)), _ptr(cnt, A.UP), nthreads)
+        return rgb, cnt
+
+    def trace(self, rays, nthreads=0):
+        rays = _f(rays)
+        tri = np.zeros(len(rays), np.int32)
+        dist = np.zeros(len(rays), np.float64)
+        orc().orc64_trace(self.h, _ptr(rays), len(rays), _ptr(tri, A.IP), dist.ctypes.data_as(C.POINTER(C.c_double)),
+                          nthreads)
+        return tri, dist
 
 
 class OrcScene:

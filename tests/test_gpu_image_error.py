@@ -1,0 +1,84 @@
+"""GPU images of the 1.18M-triangle 1080p scene against the FP64 oracle.
+
+The FP64 oracle (oracle/orc64.c) evaluates the same estimator in double on
+512 seeded pixels.  Statements (relative RMSE over those pixels,
+sqrt(sum (a - b)^2 / sum b^2), and the mean per-pixel relative MSE):
+
+1. matched samples (same seed and sample numbers, 256 spp): the FP32 GPU
+   image differs from the FP64 evaluation only by arithmetic precision and
+   the rare path that takes another branch;
+2. the 256 and 4096 spp GPU images against a converged FP64 render (4096
+   other samples per pixel): Monte Carlo error;
+3. the 8-bit-BVH batched form renders the same 256 spp image bit for bit,
+   so its error equals the plain form's.
+
+The numbers are printed (pytest -s) and bounded loosely here.
+"""
+import numpy as np
+import pytest
+
+import _oracle as O
+from eleven import _abi as A
+from eleven import _lib, scenes
+
+pytestmark = pytest.mark.gpu
+
+N_PIX, DEPTH = 512, 8
+
+
+def rel_rmse(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def rel_mse(a, b):
+    return float((((a - b) ** 2).sum(1) / ((b ** 2).sum(1) + 1e-2)).mean())
+
+
+@pytest.fixture(scope="module")
+def c1():
+    arrays = scenes.config1()
+    idx = np.sort(np.random.default_rng(3).choice(1920 * 1080, N_PIX, replace=False)).astype(np.int32)
+    orc = O.OrcScene(arrays)
+    o64 = O.Orc64(orc)
+    yield arrays, idx, o64
+    o64.close()
+    orc.close()
+
+
+def test_image_error_against_fp64_oracle(c1):
+    arrays, idx, o64 = c1
+    scene = _lib.Scene(arrays)
+    g256 = scene.render(256, max_depth=DEPTH, seed=0)["beauty"][idx, :3].astype(np.float64)
+    m256, _ = o64.render_pixels(idx, 256, DEPTH, seed=0)               # matched samples
+    ref, cnt = o64.render_pixels(idx, 4096, DEPTH, seed=0, sample_begin=1 << 20)  # independent, converged
+    g4096 = scene.render(4096, max_depth=DEPTH, seed=0)["beauty"][idx, :3].astype(np.float64)
+    scene.close()
+    out = {
+        "matched_256spp_rel_rmse": rel_rmse(g256, m256),
+        "matched_256spp_rel_mse": rel_mse(g256, m256),
+        "gpu256_vs_fp64_4096_rel_rmse": rel_rmse(g256, ref),
+        "gpu4096_vs_fp64_4096_rel_rmse": rel_rmse(g4096, ref),
+        "gpu4096_vs_fp64_4096_rel_mse": rel_mse(g4096, ref),
+        "fp64_256_vs_fp64_4096_rel_rmse": rel_rmse(m256, ref),
+    }
+    print("\nimage error vs FP64 oracle:", out)
+    assert cnt.min() > 4000
+    assert out["matched_256spp_rel_rmse"] < 0.05
+    # the GPU image is as far from the converged render as the FP64
+    # evaluation of the same samples is
+    assert out["gpu256_vs_fp64_4096_rel_rmse"] < 1.2 * out["fp64_256_vs_fp64_4096_rel_rmse"] + 1e-3
+    assert out["gpu4096_vs_fp64_4096_rel_rmse"] < out["gpu256_vs_fp64_4096_rel_rmse"]
+
+
+def test_batched_q8_image_identical_to_plain(c1):
+    arrays, idx, o64 = c1
+    plain = _lib.Scene(arrays)
+    q8 = _lib.Scene(arrays, bvh_format=A.ER_BVH_Q8)
+    a = plain.render(256, max_depth=DEPTH, seed=0)["beauty"]
+    with _lib.Batch([q8], bvh_format=A.ER_BVH_Q8) as b:
+        b.set_jobs([dict(scene=0, spp=256, max_depth=DEPTH, seed=0)])
+        b.render()
+        c = b.read(0)["beauty"]
+    assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+    plain.close()
+    q8.close()
