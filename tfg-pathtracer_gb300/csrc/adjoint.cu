@@ -14,14 +14,15 @@
 //
 // Backward: the wavefront forward first gives every sample's radiance L
 // (12 bytes per path; it sets the clamp mask and the NaN drop of the
-// accumulation, kernel.cu:445-449).  Then one thread per path re-traces the
-// path from its counter-based random numbers and scatters gradients.  At
-// vertex i the replay knows the throughput beta_i, the radiance L_<=i
-// gathered so far and therefore the radiance still to come, L - L_<=i,
-// which carries vertex i's throughput factor f_i |N.L| / pdf_i: its
-// derivative is (L - L_<=i) * df_i / f_i per channel.  Nothing per vertex is
-// stored.  Material gradients collect in shared memory per block of the
-// persistent grid, env gradients with global atomics.
+// accumulation, kernel.cu:445-449).  Then the same wavefront re-traces every
+// path from its counter-based random numbers (render.cu, gradient variants
+// of raygen and shade).  When a vertex's MIS terms are resolved, the replay
+// knows the throughput beta_i before it, the radiance L_<=i gathered so far
+// and therefore the radiance still to come, L - L_<=i, which carries vertex
+// i's throughput factor f_i |N.L| / pdf_i: its derivative is
+// (L - L_<=i) * df_i / f_i per channel (adjoint.cuh: vertex_gradient).  The
+// vertex is re-shaded from its stored hit for that; nothing else per vertex
+// is kept.  Gradients are scattered with warp-aggregated atomics.
 //
 // The same walk without gradients is a complete forward render
 // (er_render_replay): with the evaluation parameters equal to the scene's
@@ -32,148 +33,11 @@
 #include <cstring>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "internal.h"
-#include "vertex.cuh"
 
 namespace er {
 namespace {
-
-// ---------------------------------------------------------------- duals --
-// Forward-mode dual number carrying the derivative along one material
-// parameter (the replay loops over the kParams parameters of a vertex).
-constexpr int kNP = 1;
-constexpr int kParams = 5;  // albedo r, g, b, roughness, metallic
-
-struct Dual {
-  float v;
-  float d[kNP];
-};
-
-__device__ __forceinline__ Dual dconst(float v) {
-  Dual r;
-  r.v = v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = 0.f;
-  return r;
-}
-__device__ __forceinline__ Dual operator+(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v + b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] + b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator-(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v - b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] - b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v * b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v / b.v;
-  float ib = 1.0f / b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
-  return r;
-}
-__device__ __forceinline__ Dual operator+(Dual a, float b) { a.v += b; return a; }
-__device__ __forceinline__ Dual operator+(float b, Dual a) { a.v += b; return a; }
-__device__ __forceinline__ Dual operator-(float b, Dual a) {
-  Dual r;
-  r.v = b - a.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = -a.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator*(Dual a, float b) {
-  a.v *= b;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) a.d[k] *= b;
-  return a;
-}
-__device__ __forceinline__ Dual operator*(float b, Dual a) { return a * b; }
-__device__ __forceinline__ Dual operator/(Dual a, float b) { return a * (1.0f / b); }
-__device__ __forceinline__ Dual operator/(float a, Dual b) { return dconst(a) / b; }
-__device__ __forceinline__ Dual dsqrt(Dual a) {
-  Dual r;
-  r.v = sqrtf(a.v);
-  float k2 = r.v > 0.f ? 0.5f / r.v : 0.f;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] * k2;
-  return r;
-}
-// maxf_(lo, a) of the reference: lo > a ? lo : a
-__device__ __forceinline__ Dual dmax_lo(float lo, Dual a) { return lo > a.v ? dconst(lo) : a; }
-__device__ __forceinline__ Dual dlerp(Dual a, Dual b, Dual c) { return a + c * (b - a); }
-
-struct D3 {
-  Dual x, y, z;
-};
-__device__ __forceinline__ D3 d3(Dual a) { return D3{a, a, a}; }
-__device__ __forceinline__ D3 d3c(float a) { return d3(dconst(a)); }
-__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ D3 operator*(D3 a, Dual s) { return D3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ D3 operator*(D3 a, float s) { return D3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ D3 dlerp3(D3 a, D3 b, Dual c) { return D3{dlerp(a.x, b.x, c), dlerp(a.y, b.y, c), dlerp(a.z, b.z, c)}; }
-__device__ __forceinline__ D3 dlerp3(D3 a, D3 b, float c) {
-  return D3{dlerp(a.x, b.x, dconst(c)), dlerp(a.y, b.y, dconst(c)), dlerp(a.z, b.z, dconst(c))};
-}
-
-__device__ __forceinline__ Dual gtr2_aniso_d(float NDotH, float HDotX, float HDotY, Dual ax, Dual ay) {
-  Dual a = HDotX / ax, b = HDotY / ay;
-  Dual c = a * a + b * b + NDotH * NDotH;
-  return 1.0f / (ER_PI * ax * ay * c * c);
-}
-__device__ __forceinline__ Dual smith_ggx_aniso_d(float NDotV, float VDotX, float VDotY, Dual ax, Dual ay) {
-  Dual a = VDotX * ax, b = VDotY * ay;
-  return 1.0f / (NDotV + dsqrt(a * a + b * b + NDotV * NDotV));
-}
-
-// DisneyEval (Disney.hpp:179-253) with albedo, roughness and metallic as
-// duals; the other parameters and all directions are constants.
-__device__ D3 disney_eval_d(const HitData& hd, D3 Cdlin, Dual rough, Dual metal, const DisneyCtx& c, f3 L) {
-  if (!(hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f)) return d3c(0.f);
-  f3 H = normalized(L + c.V);
-  float NDotL = fabsf(dot(c.N, L));
-  float NDotV = fabsf(dot(c.N, c.V));
-  float NDotH = fabsf(dot(c.N, H));
-  float LDotH = fabsf(dot(L, H));
-  Dual Cdlum = Cdlin.x * 0.3f + Cdlin.y * 0.6f + Cdlin.z * 0.1f;
-  D3 Ctint = Cdlum.v > 0.0f ? D3{Cdlin.x / Cdlum, Cdlin.y / Cdlum, Cdlin.z / Cdlum} : d3c(1.0f);
-  D3 Cspec0 = dlerp3(dlerp3(d3c(1.0f), Ctint, hd.specularTint) * (hd.specular * 0.08f), Cdlin, metal);
-  D3 Csheen = dlerp3(d3c(1.0f), Ctint, hd.sheenTint);
-  float FL = schlick(NDotL), FV = schlick(NDotV);
-  Dual Fd90 = 0.5f + rough * (2.0f * LDotH * LDotH);
-  Dual Fd = dlerp(dconst(1.0f), Fd90, dconst(FL)) * dlerp(dconst(1.0f), Fd90, dconst(FV));
-  Dual Fss90 = rough * (LDotH * LDotH);
-  Dual Fss = dlerp(dconst(1.0f), Fss90, dconst(FL)) * dlerp(dconst(1.0f), Fss90, dconst(FV));
-  Dual ss = (Fss * (1.0f / (NDotL + NDotV) - 0.5f) + 0.5f) * 1.25f;
-  float aspect = sqrtf(1.0f - hd.anisotropic * 0.9f);
-  Dual ax = dmax_lo(0.001f, rough / aspect), ay = dmax_lo(0.001f, rough * aspect);
-  Dual Ds = gtr2_aniso_d(NDotH, dot(H, c.T), dot(H, c.B), ax, ay);
-  float FH = schlick(LDotH);
-  D3 Fs = dlerp3(Cspec0, d3c(1.0f), FH);
-  Dual Gs = smith_ggx_aniso_d(NDotL, dot(L, c.T), dot(L, c.B), ax, ay) *
-            smith_ggx_aniso_d(NDotV, dot(c.V, c.T), dot(c.V, c.B), ax, ay);
-  D3 Fsheen = Csheen * (FH * hd.sheen);
-  float Dr = gtr1(NDotH, c.clearcoatAlpha);
-  float Fr = lerpf_(0.04f, 1.0f, FH);
-  float Gr = smith_ggx(NDotL, 0.25f) * smith_ggx(NDotV, 0.25f);
-  Dual kd = dlerp(Fd, ss, dconst(hd.subsurface)) * (1.0f / ER_PI);
-  D3 diff = (Cdlin * kd + Fsheen) * (1.0f - metal);
-  D3 spec = Fs * (Gs * Ds);
-  float cc = 0.25f * hd.clearcoat * Gr * Fr * Dr;
-  return diff + spec + d3c(cc);
-}
 
 // ---------------------------------------------------------------- replay --
 
@@ -189,7 +53,6 @@ struct ReplayArgs {
   float* g_mat;              // n_mats x 5
   float* g_env;              // w*h*3
   int32_t n_mats;
-  int32_t smem_grad;         // material gradients accumulated in shared memory
   uint32_t* err;
 };
 
@@ -225,39 +88,12 @@ __device__ __forceinline__ void trace_warp(const DevScene& S, Traverser<MODE, Q8
   }
 }
 
-// base[key * N + k] += v[k], warp-aggregated: the converged lanes that
-// share a key (neighbouring pixels see the same env texel and object) are
-// summed with shuffles and one lane issues the N atomics.  Non-finite
-// contributions are dropped.
-template <int N>
-__device__ __forceinline__ void agg_add(float* base, int64_t key, float (&v)[N]) {
-#pragma unroll
-  for (int k = 0; k < N; k++)
-    if (!(fabsf(v[k]) < INFINITY)) v[k] = 0.f;
-  const unsigned active = __activemask();
-  const unsigned peers = __match_any_sync(active, (unsigned long long)key);
-  float s[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) s[k] = 0.f;
-  for (unsigned m = peers; m; m &= m - 1) {
-    const int src = __ffs(m) - 1;
-#pragma unroll
-    for (int k = 0; k < N; k++) s[k] += __shfl_sync(peers, v[k], src);
-  }
-  if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
-#pragma unroll
-    for (int k = 0; k < N; k++)
-      if (s[k] != 0.f) atomicAdd(&base[key * N + k], s[k]);
-  }
-}
-
 // One sample of pixel (x, y), called by all 32 lanes of the warp together
-// (active = false: a lane without a path this round).  GRAD = false:
-// returns the sample's radiance and vertex count.  GRAD = true: the replay,
-// given the sample's radiance Lt and its adjoint dl (d loss / d radiance).
-template <bool Q8, bool GRAD, bool EVAL>
-__device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg, bool active, int32_t x, int32_t y,
-                   uint32_t idx, uint32_t sample, f3 Lt, f3 dl, int32_t* bounces) {
+// (active = false: a lane without a path this round); returns the sample's
+// radiance and vertex count.
+template <bool Q8, bool EVAL>
+__device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, bool active, int32_t x, int32_t y,
+                   uint32_t idx, uint32_t sample, int32_t* bounces) {
   const WaveParams& P = A.P;
   uint4 ra = philox(make_uint4(idx, sample, 0u, 0u), P.k0, P.k1);
   uint4 rb = philox(make_uint4(idx, sample, 1u, 0u), P.k0, P.k1);
@@ -290,10 +126,6 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
       Lx = __fadd_rn(Lx, __fmul_rn(e.x, thr.x));
       Ly = __fadd_rn(Ly, __fmul_rn(e.y, thr.y));
       Lz = __fadd_rn(Lz, __fmul_rn(e.z, thr.z));
-      if (GRAD) {
-        float ge[3] = {dl.x * thr.x, dl.y * thr.y, dl.z * thr.z};
-        agg_add<3>(A.g_env, te, ge);
-      }
       *bounces = bounce;
       alive = false;
     }
@@ -368,52 +200,6 @@ __device__ f3 walk(const DevScene& S, const ReplayArgs& A, int2* sstk, float* sg
     Lx = __fadd_rn(Lx, __fmul_rn(__fadd_rn(__fadd_rn(hx, px), tB.x), thr.x));
     Ly = __fadd_rn(Ly, __fmul_rn(__fadd_rn(__fadd_rn(hy, py), tB.y), thr.y));
     Lz = __fadd_rn(Lz, __fmul_rn(__fadd_rn(__fadd_rn(hz, pz), tB.z), thr.z));
-    if (GRAD) {
-      // d C_i: BRDF values of the three strategies, env texel of the NEE.
-      // One parameter at a time (single-partial duals keep registers low).
-      const bool ca = M.albedo_tex < 0, cr = M.roughness_tex < 0, cm = M.metallic_tex < 0;
-      const DisneyCtx& C = V.C;
-      // strategy weights per channel: C_c = thr_c * (kH_c fH_c + kP_c fP_c + kB_c f_c)
-      const f3 kH = vH ? eH * (V.cosH / V.hdriPdf * V.w1) : mk1(0.f);
-      const f3 kB = V.hd.emission * (V.ndl / V.brdfPdf * V.w3);
-      const f3 kP = (V.has_pt && vP) ? V.plv * (V.cosP / V.pointPdf * V.w2) : mk1(0.f);
-      const f3 wd = mk(dl.x * thr.x, dl.y * thr.y, dl.z * thr.z);
-      // radiance still to come carries f_i through the throughput
-      const f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
-      const f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
-                       f.z != 0.f ? dl.z * La.z / f.z : 0.f);
-      float gk[kParams];
-#pragma unroll 1
-      for (int k = 0; k < kParams; k++) {
-        D3 alb{dconst(V.hd.albedo.x), dconst(V.hd.albedo.y), dconst(V.hd.albedo.z)};
-        Dual rg = dconst(V.hd.roughness), mt = dconst(V.hd.metallic);
-        bool seeded = false;
-        if (k == 0 && ca) { alb.x.d[0] = 1.f; seeded = true; }
-        if (k == 1 && ca) { alb.y.d[0] = 1.f; seeded = true; }
-        if (k == 2 && ca) { alb.z.d[0] = 1.f; seeded = true; }
-        if (k == 3 && cr && V.rough_in > 0.f) { rg.d[0] = 2.2f * powf(V.rough_in, 1.2f); seeded = true; }
-        if (k == 4 && cm && V.metal_in > 0.f) { mt.d[0] = 2.2f * powf(V.metal_in, 1.2f); seeded = true; }
-        float acc = 0.f;
-        if (seeded) {
-          D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
-          D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
-          acc = wd.x * (kH.x * DfH.x.d[0] + kB.x * Df.x.d[0]) + wd.y * (kH.y * DfH.y.d[0] + kB.y * Df.y.d[0]) +
-                wd.z * (kH.z * DfH.z.d[0] + kB.z * Df.z.d[0]) + ra.x * Df.x.d[0] + ra.y * Df.y.d[0] +
-                ra.z * Df.z.d[0];
-          if (V.has_pt && vP) {
-            D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
-            acc += wd.x * kP.x * DfP.x.d[0] + wd.y * kP.y * DfP.y.d[0] + wd.z * kP.z * DfP.z.d[0];
-          }
-        }
-        gk[k] = acc;
-      }
-      agg_add<kParams>(A.smem_grad ? sg : A.g_mat, V.mat, gk);
-      if (vH) {
-        float s = V.cosH / V.hdriPdf * V.w1;
-        float ge[3] = {wd.x * fH.x * s, wd.y * fH.y * s, wd.z * fH.z * s};
-        agg_add<3>(A.g_env, V.env_texel, ge);
-      }
-    }
     thr = mk(__fmul_rn(thr.x, g.x), __fmul_rn(thr.y, g.y), __fmul_rn(thr.z, g.z));
     if (bounce + 1 >= P.max_depth) break;
     // kernel.cu:442
@@ -439,8 +225,7 @@ __global__ void __launch_bounds__(kTravBlock) k_replay(DevScene S, ReplayArgs A)
   float4 bt = make_float4(0.f, 0.f, 0.f, 1.f);
   for (int32_t s = 0; s < P.spp_wave; s++) {
     int32_t nb;
-    f3 L = walk<Q8, false, EVAL>(S, A, stk + threadIdx.x, nullptr, valid, x, y, idx, (uint32_t)(P.sample_base + s),
-                                 mk1(0.f), mk1(0.f), &nb);
+    f3 L = walk<Q8, EVAL>(S, A, stk + threadIdx.x, valid, x, y, idx, (uint32_t)(P.sample_base + s), &nb);
     if (!valid) continue;
     pc += (uint32_t)nb;
     float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
@@ -461,61 +246,6 @@ __global__ void __launch_bounds__(kTravBlock) k_replay(DevScene S, ReplayArgs A)
   A.pathcount[idx] = pc;
 }
 
-#ifndef ER_BWD_MIN_BLOCKS
-#define ER_BWD_MIN_BLOCKS 2
-#endif
-// Resident blocks of 128 per SM the register budget of k_backward allows.
-constexpr int kBackwardMinBlocks = ER_BWD_MIN_BLOCKS;
-
-// Gradient replay: one path per lane over a persistent grid; each warp
-// takes 32 consecutive paths (sample-major, so neighbouring lanes trace
-// neighbouring pixels).  The sample's radiance comes from the wavefront
-// forward's per-path dump.
-template <bool Q8>
-__global__ void __launch_bounds__(kTravBlock, kBackwardMinBlocks) k_backward(DevScene S, ReplayArgs A, const float* __restrict__ rad) {
-  __shared__ int2 stk[kSmemStack * kTravBlock];
-  extern __shared__ float sg[];
-  const WaveParams& P = A.P;
-  if (A.smem_grad) {
-    for (int32_t i = threadIdx.x; i < 5 * A.n_mats; i += blockDim.x) sg[i] = 0.f;
-    __syncthreads();
-  }
-  const int64_t N = (int64_t)P.npix * P.spp_wave;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int32_t lane = (int32_t)(threadIdx.x & 31u);
-  for (int64_t base = warp * 32; base < N; base += nwarps * 32) {
-    const int64_t q = base + lane;
-    bool act = q < N;
-    const int32_t pix = act ? (int32_t)(q % P.npix) : 0, s = act ? (int32_t)(q / P.npix) : 0;
-    const int32_t x = pix % P.W, y = pix / P.W;
-    const uint32_t idx = (uint32_t)(P.W * (P.H - y - 1) + x);  // kernel.cu:378
-    f3 L = mk1(0.f), dl = mk1(0.f);
-    if (act) {
-      const uint32_t n = A.nvalid[idx];
-      const float4 g4 = A.d_beauty[idx];
-      const float* r = rad + 3 * ((int64_t)s * P.npix + idx);
-      L = mk(r[0], r[1], r[2]);
-      // dropped samples (NaN) get no gradient; clamp(L, 0, 10) passes the
-      // derivative only strictly inside
-      const float inv_n = n > 0 ? 1.0f / (float)n : 0.f;
-      const bool keep = n > 0 && !isnan(L.x) && !isnan(L.y) && !isnan(L.z);
-      dl = mk((keep && L.x > 0.f && L.x < 10.f) ? g4.x * inv_n : 0.f,
-              (keep && L.y > 0.f && L.y < 10.f) ? g4.y * inv_n : 0.f,
-              (keep && L.z > 0.f && L.z < 10.f) ? g4.z * inv_n : 0.f);
-      act = dl.x != 0.f || dl.y != 0.f || dl.z != 0.f;
-    }
-    int32_t nb;
-    walk<Q8, true, false>(S, A, stk + threadIdx.x, sg, act, x, y, idx, (uint32_t)(P.sample_base + s), L, dl, &nb);
-  }
-  if (A.smem_grad) {
-    __syncthreads();
-    for (int32_t i = threadIdx.x; i < 5 * A.n_mats; i += blockDim.x)
-      if (sg[i] != 0.f) atomicAdd(&A.g_mat[i], sg[i]);
-  }
-}
-
-constexpr int kMaxSmemGrad = 8192;  // floats of shared memory for material gradients
 
 template <bool EVAL>
 er_status launch_replay(er_scene* s, const ReplayArgs& A) {
@@ -523,20 +253,6 @@ er_status launch_replay(er_scene* s, const ReplayArgs& A) {
   const unsigned blocks = (unsigned)((npix + kTravBlock - 1) / kTravBlock);
   if (s->dev.use_q8) k_replay<true, EVAL><<<blocks, kTravBlock, 0, s->stream>>>(s->dev, A);
   else k_replay<false, EVAL><<<blocks, kTravBlock, 0, s->stream>>>(s->dev, A);
-  ER_CUDA(cudaGetLastError());
-  return ER_OK;
-}
-
-er_status launch_backward(er_scene* s, const ReplayArgs& A, const float* rad) {
-  const size_t smem = A.smem_grad ? (size_t)5 * A.n_mats * sizeof(float) : 0;
-  int occ = 0;
-  if (s->dev.use_q8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_backward<true>, kTravBlock, smem);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_backward<false>, kTravBlock, smem);
-  const int64_t N = (int64_t)A.P.npix * A.P.spp_wave;
-  const int64_t want = (N + kTravBlock - 1) / kTravBlock;
-  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(1, occ) * s->num_sms));
-  if (s->dev.use_q8) k_backward<true><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A, rad);
-  else k_backward<false><<<blocks, kTravBlock, smem, s->stream>>>(s->dev, A, rad);
   ER_CUDA(cudaGetLastError());
   return ER_OK;
 }
@@ -742,7 +458,6 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
   A.P = replay_params(s, o);
   A.n_mats = s->dev.n_mats;
   A.err = s->err_word;
-  A.smem_grad = 5 * A.n_mats <= kMaxSmemGrad;
   const size_t np = (size_t)A.P.npix;
   const size_t mat_n = (size_t)A.n_mats * 5, env_n = (size_t)s->dev.env.w * s->dev.env.h * 3;
   Temps T;
@@ -771,7 +486,14 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
     er_render_opts oo = *o;
     oo.flags &= ER_RENDER_ENV_ALIAS;
     if ((st = render_paths_device(s, &oo, d_rad, d_b)) != ER_OK) return st;
-    if ((st = launch_backward(s, A, d_rad)) != ER_OK) return st;
+    GradArgs G;
+    G.rad = d_rad;
+    G.d_beauty = A.d_beauty;
+    G.nvalid = A.nvalid;
+    G.g_mat = A.g_mat;
+    G.g_env = A.g_env;
+    G.sample0 = o->sample_begin;
+    if ((st = render_backward_device(s, &oo, G)) != ER_OK) return st;
   }
   ER_CUDA(cudaEventRecord(s->ev1, s->stream));
   if (!dev) {

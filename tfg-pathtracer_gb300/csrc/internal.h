@@ -226,6 +226,21 @@ er_status build_env_alias(er_scene* s);
 // Environment CDF and radiance sum as the reference builds them (scene.cpp).
 void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum);
 
+// Inputs and outputs of the gradient wavefront (er_backward): the forward
+// dump's per-path radiance (sample-major from sample0, output index order),
+// d loss / d beauty and the forward film's sample counts per pixel, and the
+// gradient arrays (materials x 5, env texels x 3).
+struct GradArgs {
+  const float* rad = nullptr;
+  const float4* d_beauty = nullptr;
+  const uint32_t* nvalid = nullptr;
+  float* g_mat = nullptr;
+  float* g_env = nullptr;
+  int32_t sample0 = 0;
+};
+// Runs the samples of opts through the wavefront with the gradient variant
+// of the shade stage (render.cu).
+er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G);
 // Per-path radiance (spp x npix x 3, sample-major, output index order) and
 // vertex counts of the samples er_render makes with opts, into device
 // buffers, in one wave (render.cu).

@@ -19,6 +19,7 @@
 #include "shade.cuh"
 #include "traverse.cuh"
 #include "vertex.cuh"
+#include "adjoint.cuh"
 
 namespace er {
 
@@ -31,6 +32,13 @@ struct WaveView {
   uint8_t* vis = nullptr;  // 2 per path
   int32_t* bounces = nullptr;
   float4* aovs = nullptr;  // 3 per path
+  // gradient replay (er_backward): per path the sample's radiance and its
+  // adjoint, and the last shaded vertex (origin|slot, direction|bounce, t u v)
+  float4* g_lt = nullptr;
+  float4* g_dl = nullptr;
+  float4* g_vo = nullptr;
+  float4* g_vd = nullptr;
+  float4* g_vh = nullptr;
   float4* q_o[2] = {nullptr, nullptr};
   float4* q_d[2] = {nullptr, nullptr};
   float4* hits = nullptr;
@@ -116,8 +124,19 @@ __device__ __forceinline__ int32_t path_slice(const BatchView& B, int32_t p, Wav
   return p - g.path_base;
 }
 
-template <bool BATCH>
-__global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchView B) {
+// d loss / d radiance of one sample: the pixel's adjoint spread over its
+// valid samples, zero for a dropped (NaN) sample and for clamped channels
+// (clamp(L, 0, 10) passes the derivative only strictly inside).
+__device__ __forceinline__ f3 sample_adjoint(f3 L, float4 g4, uint32_t n) {
+  const bool keep = n > 0 && !isnan(L.x) && !isnan(L.y) && !isnan(L.z);
+  const float inv_n = n > 0 ? 1.0f / (float)n : 0.f;
+  return mk((keep && L.x > 0.f && L.x < 10.f) ? g4.x * inv_n : 0.f,
+            (keep && L.y > 0.f && L.y < 10.f) ? g4.y * inv_n : 0.f,
+            (keep && L.z > 0.f && L.z < 10.f) ? g4.z * inv_n : 0.f);
+}
+
+template <bool BATCH, bool GRAD = false>
+__global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchView B, GradArgs G) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p == 0) {
     for (int k = 0; k < 16; k++) w.counts[k] = 0;
@@ -140,6 +159,13 @@ __global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchV
   w.light[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   w.pend[4 * (size_t)p + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
   w.bounces[p] = P.max_depth;
+  if (GRAD) {
+    const float* r = G.rad + 3 * ((int64_t)(sample - (uint32_t)G.sample0) * P.npix + idx);
+    const f3 L = mk(r[0], r[1], r[2]);
+    const f3 dl = sample_adjoint(L, G.d_beauty[idx], G.nvalid[idx]);
+    w.g_lt[p] = make_float4(L.x, L.y, L.z, 0.f);
+    w.g_dl[p] = make_float4(dl.x, dl.y, dl.z, 0.f);
+  }
   if (w.aov) {
     w.aovs[3 * (size_t)p] = make_float4(0, 0, 0, 0);
     w.aovs[3 * (size_t)p + 1] = make_float4(0, 0, 0, 0);
@@ -257,8 +283,30 @@ __device__ __forceinline__ void resolve(const WaveView& w, int32_t p, float4& L)
   w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
 }
 
-template <bool BATCH>
-__global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B) {
+// Gradient of the vertex whose MIS terms were just resolved (L includes
+// them): the vertex is shaded again from its stored hit, with the
+// visibility its shadow rays found.  fl = the pending flags before resolve.
+__device__ __forceinline__ void grad_prev_vertex(const DevScene& S, const WaveParams& P, const WaveView& w,
+                                                 const GradArgs& G, int32_t p, int32_t local, uint32_t fl,
+                                                 float4 L) {
+  const float4 dl4 = w.g_dl[p];
+  if (dl4.x == 0.f && dl4.y == 0.f && dl4.z == 0.f) return;
+  const float4 vo = w.g_vo[p], vd = w.g_vd[p], vh = w.g_vh[p], lt = w.g_lt[p];
+  const int32_t pix = local % P.npix, s = local / P.npix;
+  const uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
+  VertexShade V;
+  shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), __float_as_int(vd.w),
+               mk(vo.x, vo.y, vo.z), mk(vd.x, vd.y, vd.z), vh.x, vh.y, vh.z, __float_as_int(vo.w), V);
+  const float4 rp = w.pend[4 * (size_t)p + 3];
+  const bool vH = w.vis[2 * (size_t)p] != 0;
+  const bool vP = (fl & 2u) ? (w.vis[2 * (size_t)p + 1] != 0) : true;
+  vertex_gradient(S, V, mk(rp.x, rp.y, rp.z), mk(dl4.x, dl4.y, dl4.z), mk(lt.x, lt.y, lt.z), L.x, L.y, L.z, vH, vP,
+                  G.g_mat, G.g_env);
+}
+
+template <bool BATCH, bool GRAD = false>
+__global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B,
+                                               GradArgs G) {
   const int32_t qin = bounce & 1;
   const int32_t n = w.counts[kExt + qin];
   const float4* qo = w.q_o[qin];
@@ -297,14 +345,22 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WavePara
       const bool last = bounce + 1 >= P.max_depth;
       f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
       float4 L = w.light[p];
+      const uint32_t fl_prev = GRAD ? __float_as_uint(w.pend[4 * (size_t)p + 2].w) : 0u;
       resolve(w, p, L);
+      if (GRAD && (fl_prev & 1u)) grad_prev_vertex(S, P, w, G, p, local, fl_prev, L);
       float4 T4 = w.thr[p];
       f3 thr = mk(T4.x, T4.y, T4.z);
       float4 h = w.hits[i];
       int32_t slot = __float_as_int(h.w);
       if (slot < 0) {
         // kernel.cu:414-419: environment on escape, no MIS weight
-        f3 e = escape_radiance(S, d, nullptr);
+        int64_t te = 0;
+        f3 e = escape_radiance(S, d, GRAD ? &te : nullptr);
+        if (GRAD) {
+          const float4 dl4 = w.g_dl[p];
+          float ge[3] = {dl4.x * thr.x, dl4.y * thr.y, dl4.z * thr.z};
+          if (ge[0] != 0.f || ge[1] != 0.f || ge[2] != 0.f) agg_add<3>(G.g_env, te, ge);
+        }
         L.x = __fadd_rn(L.x, __fmul_rn(e.x, thr.x));
         L.y = __fadd_rn(L.y, __fmul_rn(e.y, thr.y));
         L.z = __fadd_rn(L.z, __fmul_rn(e.z, thr.z));
@@ -314,6 +370,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WavePara
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         VertexShade V;
         shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
+        if (GRAD) {
+          w.g_vo[p] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
+          w.g_vd[p] = make_float4(d.x, d.y, d.z, __int_as_float(bounce));
+          w.g_vh[p] = make_float4(h.x, h.y, h.z, 0.f);
+        }
         env_o = V.env_o;
         env_d = V.env_d;
         push_env = true;
@@ -363,6 +424,18 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WavePara
       w.s_p[j] = make_float4(pt_p.x, pt_p.y, pt_p.z, __int_as_float(job));
     }
   }
+}
+
+// Gradient of every path's last shaded vertex (resolved here instead of in
+// the accumulation).
+__global__ void k_resolve_grad(DevScene S, WaveView w, WaveParams P, int32_t n, GradArgs G) {
+  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t fl = __float_as_uint(w.pend[4 * (size_t)p + 2].w);
+  if (!(fl & 1u)) return;
+  float4 L = w.light[p];
+  resolve(w, p, L);
+  grad_prev_vertex(S, P, w, G, p, p, fl, L);
 }
 
 // kernel.cu:445-478 per pixel, samples in index order.
@@ -484,7 +557,7 @@ er_status alloc_w(Wave* w, void** p, size_t bytes) {
 
 // Allocates the buffers of `ww` for `cap` paths; on failure the caller
 // frees what was allocated.
-er_status wave_fill(Wave* ww, int64_t cap, bool aov, unsigned long long* stats) {
+er_status wave_fill(Wave* ww, int64_t cap, bool aov, bool grad, unsigned long long* stats) {
   ww->cap = cap;
   WaveView* w = &ww->v;
   w->aov = aov;
@@ -508,15 +581,22 @@ er_status wave_fill(Wave* ww, int64_t cap, bool aov, unsigned long long* stats) 
   AL(w->s_d, 2 * cap * sizeof(float4));
   AL(w->s_p, 2 * cap * sizeof(float4));
   AL(w->counts, 16 * sizeof(int32_t));
+  if (grad) {
+    AL(w->g_lt, cap * sizeof(float4));
+    AL(w->g_dl, cap * sizeof(float4));
+    AL(w->g_vo, cap * sizeof(float4));
+    AL(w->g_vd, cap * sizeof(float4));
+    AL(w->g_vh, cap * sizeof(float4));
+  }
 #undef AL
   return ER_OK;
 }
 
-er_status ensure_wave(er_scene* s, int64_t cap, bool aov) {
-  if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov)) return ER_OK;
+er_status ensure_wave(er_scene* s, int64_t cap, bool aov, bool grad = false) {
+  if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov) && (!grad || s->wave->v.g_lt)) return ER_OK;
   free_wave(s);
   s->wave = new Wave();
-  er_status st = wave_fill(s->wave, cap, aov, s->d_stats);
+  er_status st = wave_fill(s->wave, cap, aov, grad, s->d_stats);
   if (st != ER_OK) free_wave(s);
   return st;
 }
@@ -622,7 +702,7 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * npix;
-    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB);
+    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, GradArgs{});
     if ((st = mark(ER_STAGE_RAYGEN)) != ER_OK) return st;
     // trace(b): extension rays of bounce b + shadow rays of bounce b-1;
     // the extra trace(max_depth) finishes the last bounce's shadow rays.
@@ -636,7 +716,7 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
       }
       if ((st = mark(ER_STAGE_TRACE)) != ER_OK) return st;
       if (b == max_depth) break;
-      k_shade<false><<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b, NB);
+      k_shade<false><<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b, NB, GradArgs{});
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
     }
     if (dump_rad) {
@@ -685,9 +765,52 @@ er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad
   return run(s, &oo, d_rad, d_b, nullptr);
 }
 
+// The gradient wavefront: the same waves as run(), with the gradient
+// variants of raygen and shade and a final per-path resolve in place of the
+// accumulation.
+er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G) {
+  const int32_t W = s->camera.x_res, H = s->camera.y_res;
+  const int32_t npix = W * H;
+  const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
+  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : std::max(1, (int32_t)((int64_t)(1 << 22) / npix));
+  sw = std::min(sw, std::max(1, o->spp));
+  er_status st = ensure_wave(s, (int64_t)sw * npix, false, true);
+  if (st != ER_OK) return st;
+  WaveView& w = s->wave->v;
+  WaveParams P;
+  P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
+  P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
+  P.flags = o->flags & ER_RENDER_ENV_ALIAS;
+  static int g_tr[2] = {0, 0}, g_sh = 0;
+  if (!g_sh) {
+    g_tr[0] = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
+    g_tr[1] = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
+    g_sh = grid_for(k_shade<false, true>, 128, s->num_sms);
+  }
+  const BatchView NB;
+  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+    const int32_t cur = std::min(sw, o->spp - s0);
+    P.spp_wave = cur;
+    P.sample_base = o->sample_begin + s0;
+    const int32_t n = cur * npix;
+    k_raygen<false, true><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, G);
+    for (int32_t b = 0; b <= max_depth; b++) {
+      if (s->dev.use_q8)
+        k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+      else
+        k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+      if (b == max_depth) break;
+      k_shade<false, true><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB, G);
+    }
+    k_resolve_grad<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, G);
+    ER_CUDA(cudaGetLastError());
+  }
+  return ER_OK;
+}
+
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out) {
   Wave* ww = new Wave();
-  er_status st = wave_fill(ww, cap, false, stats);
+  er_status st = wave_fill(ww, cap, false, false, stats);
   if (st != ER_OK) {
     wave_destroy(ww);
     return st;
@@ -748,7 +871,7 @@ er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, cons
     B.n_segs = bw.n_segs;
     B.n_acc = bw.n_acc;
     const int32_t n = bw.n_paths;
-    k_raygen<true><<<(n + 255) / 256, 256, 0, stream>>>(S, w, P0, n, B);
+    k_raygen<true><<<(n + 255) / 256, 256, 0, stream>>>(S, w, P0, n, B, GradArgs{});
     nl++;
     for (int32_t b = 0; b <= bw.max_depth; b++) {
       if (sch.split_trace) {
@@ -759,7 +882,7 @@ er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, cons
         trace(b, B, 7u);
       }
       if (b == bw.max_depth) break;
-      k_shade<true><<<g_sh, 128, 0, stream>>>(S, w, P0, b, B);
+      k_shade<true><<<g_sh, 128, 0, stream>>>(S, w, P0, b, B, GradArgs{});
       nl++;
     }
     k_accumulate<true><<<(bw.n_acc + 127) / 128, 128, 0, stream>>>(w, P0, Film(), 0, B);
@@ -1011,14 +1134,14 @@ extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, flo
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * (int32_t)npix;
-    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB);  // also zeroes the queue counters
+    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, GradArgs{});  // also zeroes the queue counters
     for (int32_t b = 0; b <= max_depth; b++) {
       if (s->dev.use_q8)
         k_trace<true, false, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
       else
         k_trace<false, false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
       if (b == max_depth) break;
-      k_shade<false><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB);
+      k_shade<false><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB, GradArgs{});
     }
     k_accumulate<false><<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur, NB);
   }
