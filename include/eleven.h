@@ -270,6 +270,27 @@ er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
  * entries; any may be NULL.  Builds the table on first use. */
 er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
 
+/* ---------------------------------------------------------- post-process -- */
+/* The reference's PostProcessing.cpp as one GPU pass, applied in this
+ * order: applyExposure (:3-6), basicBlur bloom (:133-210), Reinhard
+ * (:37-41) or ACES (:43-55) tone map, clampPixels (:32-35), applysRGB
+ * (:57-60), flipX / flipY (:8-30).  rgba_out receives the float result,
+ * ldr_out its 8-bit encoding as er_encode_ldr makes it (either may be
+ * NULL).  flags: ER_RENDER_DEVICE_OUT for device pointers. */
+enum { ER_TONEMAP_NONE = 0, ER_TONEMAP_REINHARD = 1, ER_TONEMAP_ACES = 2 };
+
+typedef struct er_post_opts {
+  float exposure;        /* 1 = unchanged */
+  int32_t tonemap;       /* ER_TONEMAP_* */
+  int32_t clamp;         /* 1: clamp to [0, 1] */
+  int32_t srgb;          /* 1: pow(x, 1/2.2) */
+  int32_t flip_x, flip_y;
+  float bloom_threshold, bloom_power, bloom_radius;  /* bloom_power 0 = no bloom */
+} er_post_opts;
+
+er_status er_postprocess(const float* rgba_in, int32_t width, int32_t height, const er_post_opts* opts,
+                         float* rgba_out, uint8_t* ldr_out, uint32_t flags);
+
 /* --------------------------------------------------------------- adjoint -- */
 /* Differentiable parameters (no counterpart in the reference): per material
  * 5 floats (albedo r, g, b, roughness, metallic, before the 2.2 power of

@@ -150,6 +150,9 @@ void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, in
                          int32_t max_depth, uint64_t seed, double* rgb, uint32_t* counts, int32_t nthreads);
 void orc64_trace(const orc64_scene* S, const float* rays, int64_t n, int32_t* tri, double* dist, int32_t nthreads);
 
+/* ---- post-processing (PostProcessing.cpp), in place on W*H*4 floats ---- */
+void orc_postprocess(float* pix, int32_t w, int32_t h, const er_post_opts* o);
+
 /* ---- output (main.cpp:150-165) ---- */
 double orc_fastpow(double a, double b);
 void orc_encode_ldr(const float* rgba, int64_t n, uint8_t* out);

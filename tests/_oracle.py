@@ -51,6 +51,7 @@ def orc():
         _orc.orc_p_sample_u.argtypes = [C.c_void_p, C.c_int64, A.IP, C.c_int32, A.FP, A.FP]
         _orc.orc_p_philox.argtypes = [C.c_int64, A.UP, C.c_uint32, C.c_uint32, A.UP]
         _orc.orc_p_hdri_counts.argtypes = [A.FP, C.c_int32, A.UP]
+        _orc.orc_postprocess.argtypes = [A.FP, C.c_int32, C.c_int32, C.POINTER(A.er_post_opts)]
         _orc.orc64_new.restype = C.c_void_p
         _orc.orc64_new.argtypes = [C.c_void_p]
         _orc.orc64_free.argtypes = [C.c_void_p]
@@ -58,6 +59,13 @@ def orc():
                                              C.c_uint64, C.POINTER(C.c_double), A.UP, C.c_int32]
         _orc.orc64_trace.argtypes = [C.c_void_p, A.FP, C.c_int64, A.IP, C.POINTER(C.c_double), C.c_int32]
     return _orc
+
+
+def postprocess(rgba, w, h, opts):
+    """Oracle restatement of the reference's post-processing (in a copy)."""
+    px = np.array(rgba, np.float32, copy=True, order="C")
+    orc().orc_postprocess(_ptr(px), w, h, C.byref(opts))
+    return px
 
 
 def hdri_counts(cdf, n):

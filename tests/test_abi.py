@@ -39,7 +39,7 @@ def test_library_exports_in_symbol_table():
 
 STRUCTS = ["er_camera", "er_material", "er_texture", "er_point_light", "er_scene_desc", "er_scene_opts",
            "er_scene_info", "er_render_opts", "er_render_stats", "er_trace_stats", "er_batch_job",
-           "er_batch_tuning"]
+           "er_batch_tuning", "er_post_opts"]
 
 
 def test_struct_layouts(tmp_path):

@@ -171,5 +171,15 @@ EXPORTED = [
     "er_scene_get_params", "er_scene_set_params", "er_render_replay", "er_backward",
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",
-    "er_trace_closest", "er_encode_ldr", "er_write_image",
+    "er_trace_closest", "er_encode_ldr", "er_write_image", "er_postprocess",
 ]
+
+ER_TONEMAP_NONE, ER_TONEMAP_REINHARD, ER_TONEMAP_ACES = 0, 1, 2
+
+
+class er_post_opts(C.Structure):
+    _fields_ = [
+        ("exposure", C.c_float), ("tonemap", C.c_int32), ("clamp", C.c_int32), ("srgb", C.c_int32),
+        ("flip_x", C.c_int32), ("flip_y", C.c_int32),
+        ("bloom_threshold", C.c_float), ("bloom_power", C.c_float), ("bloom_radius", C.c_float),
+    ]

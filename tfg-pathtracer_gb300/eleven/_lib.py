@@ -97,6 +97,9 @@ def load(build_if_missing=True):
                                    C.c_uint32, C.POINTER(A.er_trace_stats)]
     L.er_encode_ldr.restype = A.er_status
     L.er_encode_ldr.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+    L.er_postprocess.restype = A.er_status
+    L.er_postprocess.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(A.er_post_opts), C.c_void_p,
+                                 C.c_void_p, C.c_uint32]
     L.er_write_image.restype = A.er_status
     L.er_write_image.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     _lib = L
@@ -330,6 +333,18 @@ def encode_ldr(rgba, width, height):
     out = np.zeros(width * height * 4, np.uint8)
     check(load().er_encode_ldr(_p(rgba), width, height, _p(out)), "er_encode_ldr")
     return out
+
+
+def postprocess(rgba, width, height, exposure=1.0, tonemap=0, clamp=False, srgb=False, flip_x=False, flip_y=False,
+                bloom_threshold=0.0, bloom_power=0.0, bloom_radius=0.0):
+    """GPU post-processing (er_postprocess): (float RGBA (W*H, 4), LDR bytes)."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    o = A.er_post_opts(exposure, tonemap, int(clamp), int(srgb), int(flip_x), int(flip_y), bloom_threshold,
+                       bloom_power, bloom_radius)
+    out = np.zeros((width * height, 4), np.float32)
+    ldr = np.zeros(width * height * 4, np.uint8)
+    check(load().er_postprocess(_p(rgba), width, height, C.byref(o), _p(out), _p(ldr), 0), "er_postprocess")
+    return out, ldr
 
 
 def write_image(path, rgba_u8, width, height, as_bmp=False):
