@@ -270,6 +270,15 @@ er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
  * entries; any may be NULL.  Builds the table on first use. */
 er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
 
+/* -------------------------------------------------------------- tangents -- */
+/* Per-corner tangents (9 floats per triangle) and a per-triangle sign in
+ * the manner of the MikkTSpace generator the reference's loader runs on
+ * every object (ObjLoader.hpp:167-168): welded corners, texture-space
+ * triangle tangents projected onto the corner normal's plane, angle-weighted
+ * per vertex and orientation.  er_scene_load calls it per object. */
+er_status er_compute_tangents(int64_t tri_count, const float* positions, const float* normals, const float* uvs,
+                              float* tangents, float* tangent_sign);
+
 /* ---------------------------------------------------------- post-process -- */
 /* The reference's PostProcessing.cpp as one GPU pass, applied in this
  * order: applyExposure (:3-6), basicBlur bloom (:133-210), Reinhard

@@ -137,3 +137,33 @@ def test_wave_split_is_deterministic(c0):
     a = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=4)["beauty"]
     b = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=1)["beauty"]
     assert np.array_equal(a, b)
+
+
+def test_normal_map_paths_match_oracle():
+    """Normal mapping (kernel.cu:90-100) with tangents from
+    er_compute_tangents: per-path parity with the oracle, and the AOV
+    tangent pass carries them."""
+    import dataclasses
+    arrays = scenes.config0(x_res=48, y_res=36, seed=4)
+    t, s = _lib.compute_tangents(arrays.positions, arrays.normals, arrays.uvs)
+    rng = np.random.default_rng(2)
+    nmap = np.clip(0.5 + 0.25 * rng.standard_normal((32, 32, 3)), 0, 1).astype(np.float32)
+    nmap[..., 2] = 0.9  # mostly facing out of the surface
+    mats = [dict(m) for m in arrays.materials]
+    for m in mats[::2]:
+        m["normal_tex"] = 0
+    arrays = dataclasses.replace(arrays, tangents=t, tangent_sign=s, textures=[nmap], materials=mats)
+    scene = _lib.Scene(arrays)
+    orc = O.OrcScene(arrays)
+    rad, b = scene.render_paths(spp=2, max_depth=4, seed=5)
+    rrad, rb = orc.render_paths(spp=2, max_depth=4, seed=5)
+    close = np.isclose(rad, rrad, rtol=1e-3, atol=1e-5).all(axis=2)
+    both_nan = np.isnan(rad).any(2) & np.isnan(rrad).any(2)
+    assert (b == rb).mean() > 0.99
+    assert (close | both_nan).mean() > 0.98
+    out = scene.render(spp=1, max_depth=2, seed=5, aov=True)
+    ref = orc.render(spp=1, max_depth=2, seed=5, aov=True)
+    assert np.abs(out["tangent"][:, :3]).max() > 0.5
+    np.testing.assert_allclose(out["tangent"][:, :3], ref["tangent"][:, :3], rtol=1e-4, atol=1e-5)
+    scene.close()
+    orc.close()

@@ -223,6 +223,9 @@ void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
 er_status build_env_alias(er_scene* s);
+// Per-corner tangents and per-triangle signs (tangents.cpp).
+void compute_tangents(int64_t n_tris, const float* pos, const float* nrm, const float* uv, float* tangents,
+                      float* sign);
 // Environment CDF and radiance sum as the reference builds them (scene.cpp).
 void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum);
 

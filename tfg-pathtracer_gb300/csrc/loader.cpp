@@ -659,6 +659,17 @@ extern "C" er_status er_scene_load(const char* dir_c, const er_scene_opts* opts,
   d.positions = pos.data();
   d.normals = nrm.data();
   d.uvs = uv.data();
+  // tangents per object, as the reference's loader does (ObjLoader.hpp:167-168)
+  std::vector<float> tan(pos.size()), tsign((size_t)d.tri_count);
+  for (int64_t b = 0, o = 0; b < d.tri_count; o++) {
+    int64_t e = b;
+    while (e < d.tri_count && tri_obj[(size_t)e] == o) e++;
+    compute_tangents(e - b, pos.data() + 9 * b, nrm.data() + 9 * b, uv.data() + 6 * b, tan.data() + 9 * b,
+                     tsign.data() + b);
+    b = e;
+  }
+  d.tangents = tan.data();
+  d.tangent_sign = tsign.data();
   d.tri_object = tri_obj.data();
   d.object_count = (int32_t)obj_mat.size();
   d.object_material = obj_mat.data();

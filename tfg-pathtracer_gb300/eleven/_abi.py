@@ -171,7 +171,7 @@ EXPORTED = [
     "er_scene_get_params", "er_scene_set_params", "er_render_replay", "er_backward",
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",
-    "er_trace_closest", "er_encode_ldr", "er_write_image", "er_postprocess",
+    "er_trace_closest", "er_encode_ldr", "er_write_image", "er_postprocess", "er_compute_tangents",
 ]
 
 ER_TONEMAP_NONE, ER_TONEMAP_REINHARD, ER_TONEMAP_ACES = 0, 1, 2

@@ -97,6 +97,8 @@ def load(build_if_missing=True):
                                    C.c_uint32, C.POINTER(A.er_trace_stats)]
     L.er_encode_ldr.restype = A.er_status
     L.er_encode_ldr.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+    L.er_compute_tangents.restype = A.er_status
+    L.er_compute_tangents.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_postprocess.restype = A.er_status
     L.er_postprocess.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(A.er_post_opts), C.c_void_p,
                                  C.c_void_p, C.c_uint32]
@@ -333,6 +335,17 @@ def encode_ldr(rgba, width, height):
     out = np.zeros(width * height * 4, np.uint8)
     check(load().er_encode_ldr(_p(rgba), width, height, _p(out)), "er_encode_ldr")
     return out
+
+
+def compute_tangents(positions, normals, uvs):
+    """Per-corner tangents (T, 3, 3) and per-triangle signs (T,) (er_compute_tangents)."""
+    P = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
+    N = np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    U = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6)
+    t = np.zeros((len(P), 3, 3), np.float32)
+    s = np.zeros(len(P), np.float32)
+    check(load().er_compute_tangents(len(P), _p(P), _p(N), _p(U), _p(t), _p(s)), "er_compute_tangents")
+    return t, s
 
 
 def postprocess(rgba, width, height, exposure=1.0, tonemap=0, clamp=False, srgb=False, flip_x=False, flip_y=False,

@@ -32,7 +32,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcom
 # extra nvcc flags (tuning sweeps); a change needs build_product(force=True)
 CU_FLAGS += os.environ.get("ELEVEN_NVCC_FLAGS", "").split()
 
-SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp",
+SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp", "tangents.cpp",
            "trace.cu", "render.cu", "env.cu", "batch.cu", "adjoint.cu", "post.cu"]
 
 
