@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--jobs", type=int, default=64, help="c2: number of batch jobs")
     ap.add_argument("--bvh", default="fp32", choices=["fp32", "q8"])
     ap.add_argument("--max-leaf", type=int, default=0, help="triangles per BVH leaf (0 = library default)")
+    ap.add_argument("--builder", default="host", choices=["host", "gpu"], help="BVH builder")
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -231,7 +232,8 @@ def run_gpu(args):
     W, H = arrays.camera["x_res"], arrays.camera["y_res"]
     npix = W * H
     fmt = A.ER_BVH_Q8 if args.bvh == "q8" else A.ER_BVH_FP32
-    scene = _lib.Scene(arrays, bvh_format=fmt, max_leaf=args.max_leaf, device=local)
+    builder = A.ER_BUILDER_GPU if args.builder == "gpu" else A.ER_BUILDER_HOST
+    scene = _lib.Scene(arrays, bvh_format=fmt, max_leaf=args.max_leaf, device=local, builder=builder)
     info = scene.info()
     base = rank * (args.warmup + args.steps + args.e2e_steps + 8)
 
@@ -295,7 +297,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, reference scene shapes)",
-        "config": dict(cfg, spp_per_step=1, bvh=args.bvh, max_leaf_tris=args.max_leaf or 4,
+        "config": dict(cfg, spp_per_step=1, bvh=args.bvh, max_leaf_tris=args.max_leaf or 4, bvh_builder=args.builder,
                        triangles=arrays.tri_count,
                        l2="working set > 126 MB L2 (no flush)", parallelism="replicas" if world > 1 else "1 GPU"),
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(C.sizeof(A.er_render_opts)),

@@ -127,11 +127,17 @@ typedef struct er_scene_desc {
 /* BVH node formats. */
 enum { ER_BVH_FP32 = 0, ER_BVH_Q8 = 1 };
 
+/* BVH builders: the host SAH builder (default; slower to build, faster to
+ * trace) or the GPU linear BVH (Morton order, ~100x faster to build).  The
+ * hit set does not depend on the builder. */
+enum { ER_BUILDER_HOST = 0, ER_BUILDER_GPU = 1 };
+
 typedef struct er_scene_opts {
   int32_t bvh_format;     /* ER_BVH_FP32 or ER_BVH_Q8 */
   int32_t max_leaf_tris;  /* 1..8, 0 = default (4) */
   int32_t device;         /* CUDA device ordinal */
   void* stream;           /* cudaStream_t, NULL = handle-owned stream */
+  int32_t builder;        /* ER_BUILDER_HOST or ER_BUILDER_GPU */
 } er_scene_opts;
 
 typedef struct er_scene er_scene;

@@ -68,6 +68,22 @@ struct BuildResult {
   float max_delta = 0;
 };
 
+// A BVH4 built on the device (bvh_gpu.cu): node and leaf-order triangle
+// arrays allocated on the scene.
+struct GpuBvh {
+  const float4* nodes;
+  const float4* tri_v;
+  const float4* tri_n;
+  const float2* tri_uv;
+  const float4* tri_t;
+  int64_t node_count, leaf_count;
+  int32_t depth;
+  float max_delta;
+  double build_ms;
+};
+er_status build_bvh_gpu(er_scene* s, const er_scene_desc* d, int max_leaf, const float scene_lo[3],
+                        const float scene_hi[3], GpuBvh* out);
+
 // Builds the SAH BVH4 over the desc's triangles (bvh_build.cpp).
 er_status build_bvh4(const er_scene_desc* d, int max_leaf, BuildResult* out);
 void quantize_bvh4(BuildResult* r);

@@ -183,6 +183,7 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   o.bvh_format = ER_BVH_FP32;
   if (opts) o = *opts;
   if (o.bvh_format != ER_BVH_FP32 && o.bvh_format != ER_BVH_Q8) return fail(ER_ERR_INVALID_ARG, "bvh_format");
+  if (o.builder != ER_BUILDER_HOST && o.builder != ER_BUILDER_GPU) return fail(ER_ERR_INVALID_ARG, "builder");
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev == 0) {
@@ -214,22 +215,32 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   cudaEventCreate(&s->ev1);
 
   // ---- BVH
+  const bool gpu_build = o.builder == ER_BUILDER_GPU;
   auto t0 = std::chrono::steady_clock::now();
   BuildResult br;
-  st = build_bvh4(d, o.max_leaf_tris > 0 ? o.max_leaf_tris : 4, &br);
-  if (st != ER_OK) return bail(st);
-  if (3 * br.depth + 1 > 96) return bail(fail(ER_ERR_UNSUPPORTED, "BVH too deep for the traversal stack"));
-  if (o.bvh_format == ER_BVH_Q8) quantize_bvh4(&br);
+  if (!gpu_build) {
+    st = build_bvh4(d, o.max_leaf_tris > 0 ? o.max_leaf_tris : 4, &br);
+    if (st != ER_OK) return bail(st);
+    if (3 * br.depth + 1 > 96) return bail(fail(ER_ERR_UNSUPPORTED, "BVH too deep for the traversal stack"));
+    if (o.bvh_format == ER_BVH_Q8) quantize_bvh4(&br);
+  }
   auto t1 = std::chrono::steady_clock::now();
 
-  // ---- leaf-ordered triangle data
+  // ---- leaf-ordered triangle data (the GPU builder gathers its own)
   int64_t T = d->tri_count;
-  std::vector<float4> tv((size_t)(3 * std::max<int64_t>(T, 1))), tn((size_t)(3 * std::max<int64_t>(T, 1)));
-  std::vector<float2> tuv((size_t)(3 * std::max<int64_t>(T, 1)));
+  const int64_t T_host = gpu_build ? 0 : T;
+  std::vector<float4> tv((size_t)(3 * std::max<int64_t>(T_host, 1))), tn((size_t)(3 * std::max<int64_t>(T_host, 1)));
+  std::vector<float2> tuv((size_t)(3 * std::max<int64_t>(T_host, 1)));
   std::vector<float4> tt;
-  if (d->tangents) tt.resize((size_t)(3 * T));
+  if (d->tangents && !gpu_build) tt.resize((size_t)(3 * T));
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int64_t s_ = 0; s_ < T; s_++) {
+  if (gpu_build)
+    for (int64_t i = 0; i < 3 * T; i++)
+      for (int a = 0; a < 3; a++) {
+        lo[a] = std::min(lo[a], d->positions[3 * i + a]);
+        hi[a] = std::max(hi[a], d->positions[3 * i + a]);
+      }
+  for (int64_t s_ = 0; s_ < T_host; s_++) {
     int32_t i = br.order[(size_t)s_];
     const float* p = d->positions + 9 * (int64_t)i;
     int32_t obj = d->tri_object ? d->tri_object[i] : 0;
@@ -286,14 +297,41 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   void *p_nodes = nullptr, *p_q = nullptr, *p_tv, *p_tn, *p_tuv, *p_tt = nullptr, *p_mats, *p_texs, *p_pool, *p_cdf,
        *p_lights, *p_err;
   auto t2 = std::chrono::steady_clock::now();
-  if ((st = upload(s, &p_nodes, br.nodes.data(), br.nodes.size() * sizeof(float))) != ER_OK) return bail(st);
+  double gpu_build_ms = 0;
+  if (gpu_build) {
+    GpuBvh g{};
+    float blo[3], bhi[3];
+    for (int a = 0; a < 3; a++) { blo[a] = T > 0 ? lo[a] : 0.f; bhi[a] = T > 0 ? hi[a] : 0.f; }
+    if ((st = build_bvh_gpu(s, d, o.max_leaf_tris > 0 ? o.max_leaf_tris : 4, blo, bhi, &g)) != ER_OK) return bail(st);
+    if (3 * g.depth + 1 > 96) return bail(fail(ER_ERR_UNSUPPORTED, "BVH too deep for the traversal stack"));
+    p_nodes = (void*)g.nodes;
+    p_tv = (void*)g.tri_v;
+    p_tn = (void*)g.tri_n;
+    p_tuv = (void*)g.tri_uv;
+    p_tt = (void*)g.tri_t;
+    br.node_count = g.node_count;
+    br.leaf_count = g.leaf_count;
+    br.depth = g.depth;
+    br.max_delta = g.max_delta;
+    gpu_build_ms = g.build_ms;
+    if (o.bvh_format == ER_BVH_Q8) {
+      // quantised from the GPU tree on the host (outward rounding checked
+      // with the kernel's float operations)
+      br.nodes.resize((size_t)g.node_count * 32);
+      ce = cudaMemcpy(br.nodes.data(), g.nodes, br.nodes.size() * sizeof(float), cudaMemcpyDeviceToHost);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "BVH download"));
+      quantize_bvh4(&br);
+    }
+  } else {
+    if ((st = upload(s, &p_nodes, br.nodes.data(), br.nodes.size() * sizeof(float))) != ER_OK) return bail(st);
+    if ((st = upload(s, &p_tv, tv.data(), tv.size() * sizeof(float4))) != ER_OK) return bail(st);
+    if ((st = upload(s, &p_tn, tn.data(), tn.size() * sizeof(float4))) != ER_OK) return bail(st);
+    if ((st = upload(s, &p_tuv, tuv.data(), tuv.size() * sizeof(float2))) != ER_OK) return bail(st);
+    if (d->tangents && (st = upload(s, &p_tt, tt.data(), tt.size() * sizeof(float4))) != ER_OK) return bail(st);
+  }
   if (o.bvh_format == ER_BVH_Q8 &&
       (st = upload(s, &p_q, br.qnodes.data(), br.qnodes.size() * sizeof(QNode))) != ER_OK)
     return bail(st);
-  if ((st = upload(s, &p_tv, tv.data(), tv.size() * sizeof(float4))) != ER_OK) return bail(st);
-  if ((st = upload(s, &p_tn, tn.data(), tn.size() * sizeof(float4))) != ER_OK) return bail(st);
-  if ((st = upload(s, &p_tuv, tuv.data(), tuv.size() * sizeof(float2))) != ER_OK) return bail(st);
-  if (d->tangents && (st = upload(s, &p_tt, tt.data(), tt.size() * sizeof(float4))) != ER_OK) return bail(st);
   if ((st = upload(s, &p_mats, mats.data(), mats.size() * sizeof(DevMaterial))) != ER_OK) return bail(st);
   if ((st = upload(s, &p_texs, texs.data(), texs.size() * sizeof(DevTex))) != ER_OK) return bail(st);
   if ((st = upload(s, &p_pool, pool.data(), pool.size() * sizeof(float4))) != ER_OK) return bail(st);
@@ -341,7 +379,7 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   I.tri_count = T;
   I.node_count = br.node_count;
   I.leaf_count = br.leaf_count;
-  I.bvh_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  I.bvh_build_ms = gpu_build ? gpu_build_ms : std::chrono::duration<double, std::milli>(t1 - t0).count();
   I.upload_ms = std::chrono::duration<double, std::milli>(t3 - t2).count();
   I.max_shading_offset = br.max_delta;
   I.bvh_depth = br.depth;

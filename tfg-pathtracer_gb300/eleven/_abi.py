@@ -95,10 +95,14 @@ class er_scene_desc(C.Structure):
     ]
 
 
+ER_BUILDER_HOST = 0
+ER_BUILDER_GPU = 1
+
+
 class er_scene_opts(C.Structure):
     _fields_ = [
         ("bvh_format", C.c_int32), ("max_leaf_tris", C.c_int32),
-        ("device", C.c_int32), ("stream", C.c_void_p),
+        ("device", C.c_int32), ("stream", C.c_void_p), ("builder", C.c_int32),
     ]
 
 

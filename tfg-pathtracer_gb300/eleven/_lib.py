@@ -120,14 +120,15 @@ def _p(a):
 class Scene:
     """A scene handle on the GPU (er_scene)."""
 
-    def __init__(self, arrays=None, bvh_format=A.ER_BVH_FP32, max_leaf=0, device=0, stream=None, handle=None):
+    def __init__(self, arrays=None, bvh_format=A.ER_BVH_FP32, max_leaf=0, device=0, stream=None, handle=None,
+                 builder=A.ER_BUILDER_HOST):
         L = load()
         self.arrays = arrays
         if handle is not None:
             self.h = handle
             return
         desc, keep = arrays.desc()
-        opts = A.er_scene_opts(bvh_format, max_leaf, device, stream)
+        opts = A.er_scene_opts(bvh_format, max_leaf, device, stream, builder)
         h = C.c_void_p()
         check(L.er_scene_create(C.byref(desc), C.byref(opts), C.byref(h)), "er_scene_create")
         self.h = h

@@ -33,7 +33,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcom
 CU_FLAGS += os.environ.get("ELEVEN_NVCC_FLAGS", "").split()
 
 SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp", "tangents.cpp",
-           "trace.cu", "render.cu", "env.cu", "batch.cu", "adjoint.cu", "post.cu"]
+           "trace.cu", "render.cu", "env.cu", "batch.cu", "adjoint.cu", "post.cu", "bvh_gpu.cu"]
 
 
 def _run(cmd, cwd=None):
