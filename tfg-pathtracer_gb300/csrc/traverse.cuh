@@ -30,8 +30,11 @@ constexpr int kTravBlock = 128;
 #define ER_TRAV_MIN_BLOCKS 7
 #endif
 constexpr int kTravMinBlocks = ER_TRAV_MIN_BLOCKS;  // blocks of 128 per SM the register budget allows
-constexpr int kSmemStack = 16;
-constexpr int kLocalStack = 80;
+#ifndef ER_SMEM_STACK
+#define ER_SMEM_STACK 16
+#endif
+constexpr int kSmemStack = ER_SMEM_STACK;   // stack entries per lane in shared memory
+constexpr int kLocalStack = 96 - kSmemStack;  // the rest in local memory
 constexpr int kMaxStack = kSmemStack + kLocalStack;
 
 struct TravStats {
