@@ -188,7 +188,9 @@ enum {
                                      call instead of clearing it            */
   ER_RENDER_NO_OUTPUT = 1u << 5,  /* render into the film only              */
   ER_RENDER_PROFILE = 1u << 6,    /* CUDA-event time per stage (stats)      */
-  ER_RENDER_COUNT = 1u << 7       /* count node visits / triangle tests     */
+  ER_RENDER_COUNT = 1u << 7,      /* count node visits / triangle tests     */
+  ER_RENDER_SNAPSHOTS = 1u << 8   /* copy the film to the snapshot buffer
+                                     after every wave (er_snapshot)         */
 };
 
 /* Stages of the wavefront, indices of er_render_stats.stage_ms.  TRACE is
@@ -236,6 +238,15 @@ er_status er_render(er_scene* scene, const er_render_opts* opts, float* beauty,
 er_status er_film_read(er_scene* scene, uint32_t flags, float* beauty,
                        float* normal, float* tangent, float* bitangent,
                        uint32_t* samples, uint32_t* pathcount);
+
+/* Progressive readback while er_render runs on another thread (the
+ * reference's window loop polls getBuffers during renderCuda, main.cpp:53,
+ * kernel.cu:688-710): the film as of the last finished wave of a render
+ * made with ER_RENDER_SNAPSHOTS (beauty RGBA float and per-pixel sample
+ * counts, host pointers; either may be NULL).  The only call that may run
+ * concurrently with another call on the same scene; it uses its own
+ * stream.  ER_ERR_INVALID_ARG until a first wave has finished. */
+er_status er_snapshot(er_scene* scene, float* beauty, uint32_t* samples);
 
 /* Allocation-free render.  No counterpart in the reference: it is for
  * callers that may not allocate device memory while rendering (a host

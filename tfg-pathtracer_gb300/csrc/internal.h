@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -229,6 +230,14 @@ struct er_scene {
   const uint32_t* env_counts = nullptr;   // effective env texel counts (env.cu)
   int64_t texel_count = 0;                // float4 entries of dev.texels (textures + env)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // progressive readback (er_snapshot): a copy of the film after each wave
+  std::mutex snap_mu;
+  float4* snap_beauty = nullptr;
+  uint32_t* snap_samples = nullptr;
+  int32_t snap_w = 0, snap_h = 0;
+  bool snap_valid = false;
+  cudaEvent_t snap_event = nullptr;
+  cudaStream_t snap_stream = nullptr;
 };
 
 namespace er {

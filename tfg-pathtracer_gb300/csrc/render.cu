@@ -724,11 +724,44 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     } else {
       Film F = s->film;
       k_accumulate<false><<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur, NB);
+      if (o->flags & ER_RENDER_SNAPSHOTS) {
+        // the reader (er_snapshot) holds the lock while it copies the
+        // snapshot out, so the buffer is not overwritten under it
+        std::lock_guard<std::mutex> lk(s->snap_mu);
+        ER_CUDA(cudaMemcpyAsync(s->snap_beauty, F.beauty, (size_t)npix * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                s->stream));
+        ER_CUDA(cudaMemcpyAsync(s->snap_samples, F.samples, (size_t)npix * 4, cudaMemcpyDeviceToDevice, s->stream));
+        ER_CUDA(cudaEventRecord(s->snap_event, s->stream));
+        s->snap_valid = true;
+      }
     }
     if ((st = mark(ER_STAGE_ACCUMULATE)) != ER_OK) return st;
     ER_CUDA(cudaGetLastError());
   }
   if (launches) *launches = nl;
+  return ER_OK;
+}
+
+// Snapshot buffer, event and reader stream of the scene's film size.
+er_status ensure_snapshot(er_scene* s) {
+  std::lock_guard<std::mutex> lk(s->snap_mu);
+  const int32_t W = s->camera.x_res, H = s->camera.y_res;
+  if (s->snap_beauty && s->snap_w == W && s->snap_h == H) return ER_OK;
+  cudaFree(s->snap_beauty);
+  cudaFree(s->snap_samples);
+  s->snap_beauty = nullptr;
+  s->snap_samples = nullptr;
+  s->snap_valid = false;
+  const size_t np = (size_t)W * H;
+  if (cudaMalloc(&s->snap_beauty, np * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&s->snap_samples, np * 4) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ER_ERR_OOM, "snapshot buffers");
+  }
+  if (!s->snap_event) ER_CUDA(cudaEventCreateWithFlags(&s->snap_event, cudaEventDisableTiming));
+  if (!s->snap_stream) ER_CUDA(cudaStreamCreateWithFlags(&s->snap_stream, cudaStreamNonBlocking));
+  s->snap_w = W;
+  s->snap_h = H;
   return ER_OK;
 }
 
@@ -761,7 +794,7 @@ void free_film(er_scene* s) {
 
 er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b) {
   er_render_opts oo = *o;
-  oo.flags &= ~(uint32_t)ER_RENDER_AOV;
+  oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
   return run(s, &oo, d_rad, d_b, nullptr);
 }
 
@@ -918,6 +951,19 @@ extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, fl
   return ER_OK;
 }
 
+extern "C" er_status er_snapshot(er_scene* s, float* beauty, uint32_t* samples) {
+  if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+  ER_CUDA(cudaSetDevice(s->device));
+  std::lock_guard<std::mutex> lk(s->snap_mu);
+  if (!s->snap_valid) return fail(ER_ERR_INVALID_ARG, "no snapshot yet (render with ER_RENDER_SNAPSHOTS)");
+  const size_t np = (size_t)s->snap_w * s->snap_h;
+  ER_CUDA(cudaStreamWaitEvent(s->snap_stream, s->snap_event, 0));
+  if (beauty) ER_CUDA(cudaMemcpyAsync(beauty, s->snap_beauty, np * sizeof(float4), cudaMemcpyDeviceToHost, s->snap_stream));
+  if (samples) ER_CUDA(cudaMemcpyAsync(samples, s->snap_samples, np * 4, cudaMemcpyDeviceToHost, s->snap_stream));
+  ER_CUDA(cudaStreamSynchronize(s->snap_stream));
+  return ER_OK;
+}
+
 extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beauty, float* normal, float* tangent,
                                float* bitangent, uint32_t* samples, uint32_t* pathcount, er_render_stats* stats) {
   er_status st = check_opts(s, o);
@@ -926,6 +972,7 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
   const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
   if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
   if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
+  if ((o->flags & ER_RENDER_SNAPSHOTS) && (st = ensure_snapshot(s)) != ER_OK) return st;
   unsigned long long st0[8];
   ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
   ER_CUDA(cudaEventRecord(s->ev0, s->stream));
@@ -980,7 +1027,7 @@ extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float
     return fail(ER_ERR_OOM, "path dump allocation failed");
   }
   er_render_opts oo = *o;
-  oo.flags &= ~(uint32_t)ER_RENDER_AOV;
+  oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
   if ((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) {
     cudaFree(d_rad);
     cudaFree(d_b);

@@ -425,6 +425,10 @@ extern "C" er_status er_scene_free(er_scene* s) {
   for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
+  cudaFree(s->snap_beauty);
+  cudaFree(s->snap_samples);
+  if (s->snap_event) cudaEventDestroy(s->snap_event);
+  if (s->snap_stream) cudaStreamDestroy(s->snap_stream);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return ER_OK;

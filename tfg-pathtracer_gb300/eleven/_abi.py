@@ -129,6 +129,7 @@ class er_render_opts(C.Structure):
 
 ER_RENDER_PROFILE = 1 << 6
 ER_RENDER_COUNT = 1 << 7
+ER_RENDER_SNAPSHOTS = 1 << 8
 STAGES = ["raygen", "trace", "shade", "reserved", "accumulate"]
 
 
@@ -171,7 +172,7 @@ EXPORTED = [
     "er_status_string", "er_last_error", "er_abi_version",
     "er_scene_create", "er_scene_load", "er_scene_info_get",
     "er_scene_set_camera", "er_scene_get_camera", "er_scene_free",
-    "er_render", "er_film_read", "er_render_paths", "er_render_noalloc", "er_env_distribution",
+    "er_render", "er_film_read", "er_snapshot", "er_render_paths", "er_render_noalloc", "er_env_distribution",
     "er_scene_get_params", "er_scene_set_params", "er_render_replay", "er_backward",
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",

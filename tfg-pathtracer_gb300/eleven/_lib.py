@@ -61,6 +61,8 @@ def load(build_if_missing=True):
     L.er_film_read.restype = A.er_status
     L.er_film_read.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p]
+    L.er_snapshot.restype = A.er_status
+    L.er_snapshot.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_env_distribution.restype = A.er_status
     L.er_env_distribution.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_render_noalloc.restype = A.er_status
@@ -251,6 +253,15 @@ class Scene:
         st = A.er_render_stats()
         check(load().er_backward(self.h, C.byref(o), _p(db), _p(sa), _p(gm), _p(ge), C.byref(st)), "er_backward")
         return gm, ge, st
+
+    def snapshot(self):
+        """Film as of the last finished wave of a render running with
+        ER_RENDER_SNAPSHOTS (callable from another thread): (beauty, samples)."""
+        W, H = self.resolution
+        beauty = np.zeros((H * W, 4), np.float32)
+        samples = np.zeros(H * W, np.uint32)
+        check(load().er_snapshot(self.h, _p(beauty), _p(samples)), "er_snapshot")
+        return beauty, samples
 
     def render_paths(self, spp, max_depth=5, seed=0, sample_begin=0):
         W, H = self.resolution
