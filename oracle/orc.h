@@ -149,6 +149,12 @@ void orc64_free(orc64_scene* S);
 void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
                          int32_t max_depth, uint64_t seed, double* rgb, uint32_t* counts, int32_t nthreads);
 void orc64_trace(const orc64_scene* S, const float* rays, int64_t n, int32_t* tri, double* dist, int32_t nthreads);
+/* the detached estimator: sampling from the scene, BRDF values and env
+ * radiance from eval_mat (n_materials x 5) / eval_env (w*h*3), NULL = the
+ * scene's (as er_render_replay) */
+void orc64_render_pixels_eval(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
+                              int32_t max_depth, uint64_t seed, const float* eval_mat, const float* eval_env,
+                              double* rgb, uint32_t* counts, int32_t nthreads);
 
 /* ---- post-processing (PostProcessing.cpp), in place on W*H*4 floats ---- */
 void orc_postprocess(float* pix, int32_t w, int32_t h, const er_post_opts* o);

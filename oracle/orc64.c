@@ -281,6 +281,32 @@ static hit64 closest(const orc64_scene* S, const ray64* r) {
 
 /* ------------------------------------------------------------- shading */
 
+/* Evaluation parameters of the detached estimator (as er_render_replay):
+ * sampling uses the scene's materials and environment, BRDF values and
+ * environment radiance these (NULL = the scene's). */
+typedef struct {
+  const float* mat; /* n_materials x 5: albedo rgb, roughness, metallic */
+  const float* env; /* env w*h*3, storage order */
+} eval64;
+
+/* storage index of the texel orc_tex_coord reads (Texture.hpp:95-112) */
+static int64_t tex_index64(const orc_tex* t, int32_t x, int32_t y) {
+  x = f2i_dev(t->xTile * ((float)x + t->xOffset * (float)t->w)) % t->w;
+  y = f2i_dev(t->yTile * ((float)y + t->yOffset * (float)t->h)) % t->h;
+  if (x < 0) x += t->w;
+  if (y < 0) y += t->h;
+  return (int64_t)y * t->w + x;
+}
+
+static d3 env_value64(const orc_tex* t, const eval64* ev, double u, double v) {
+  int32_t x = d2i(u * (double)t->w), y = d2i(v * (double)t->h);
+  if (ev && ev->env) {
+    const float* p = ev->env + 3 * tex_index64(t, x, y);
+    return D(p[0], p[1], p[2]);
+  }
+  return Df(orc_tex_coord(t, x, y));
+}
+
 typedef struct {
   double metallic, roughness, clearcoatGloss, clearcoat, anisotropic, transmission, specular, specularTint,
       sheenTint, subsurface, sheen;
@@ -330,6 +356,16 @@ static void hit_data64(const orc_scene* s, const er_material* m, const hit64* h,
   hd->sheenTint = m->sheen_tint;
   hd->subsurface = m->subsurface;
   hd->sheen = m->sheen;
+}
+
+/* the evaluation copy of a vertex's HitData */
+static void hit_data_eval64(const er_material* m, int32_t mat_id, const eval64* ev, const hd64* hs, hd64* he) {
+  *he = *hs;
+  if (!ev || !ev->mat) return;
+  const float* q = ev->mat + 5 * (int64_t)mat_id;
+  if (m->albedo_tex < 0) he->albedo = D(q[0], q[1], q[2]);
+  if (m->roughness_tex < 0) he->roughness = pow((double)q[3], 2.2);
+  if (m->metallic_tex < 0) he->metallic = pow((double)q[4], 2.2);
 }
 
 static void basis64(d3 n, d3* t, d3* b) {
@@ -460,7 +496,8 @@ static ray64 camera64(const er_camera* c, int32_t x, int32_t y, const double* u)
 }
 
 /* kernel.cu:175-205 */
-static d3 point_light64(const orc64_scene* S, const ray64* r, const hd64* hd, d3 p, double* pdf, float r1) {
+static d3 point_light64(const orc64_scene* S, const ray64* r, const hd64* hd, const hd64* he, d3 p, double* pdf,
+                        float r1) {
   const orc_scene* s = S->s;
   if (s->nlights <= 0) { *pdf = 0; return D(0, 0, 0); }
   *pdf = s->nlights / (2.0 * PI64);
@@ -474,12 +511,13 @@ static d3 point_light64(const orc64_scene* S, const ray64* r, const hd64* hd, d3
   hit64 sh = closest(S, &sr);
   if (sh.valid && len(sub(sh.position, p)) < dist) return D(0, 0, 0);
   d3 plv = dvs(D(L->radiance[0], L->radiance[1], L->radiance[2]), dist * dist);
-  d3 f = disney_eval64(r, hd, dir);
+  d3 f = disney_eval64(r, he, dir);
   return dvs(scl(mul(plv, f), fabs(dot(dir, hd->normal))), *pdf);
 }
 
 /* kernel.cu:210-258, texel chosen as the FP32 renderers choose it */
-static d3 hdri_light64(const orc64_scene* S, const ray64* r, d3 p, const hd64* hd, float r1, double* pdf) {
+static d3 hdri_light64(const orc64_scene* S, const ray64* r, d3 p, const hd64* hd, const hd64* he, const eval64* ev,
+                       float r1, double* pdf) {
   const orc_scene* s = S->s;
   const orc_tex* t = &s->env;
   int32_t count = orc_hdri_search(s->cdf, r1, t->w * t->h);
@@ -497,14 +535,14 @@ static d3 hdri_light64(const orc64_scene* S, const ray64* r, d3 p, const hd64* h
   ray64 sr = make_ray(add(p, scl(dir, 0.001)), dir);
   hit64 sh = closest(S, &sr);
   if (sh.valid) return D(0, 0, 0);
-  d3 hv = tex_uv64(t, iu, iv);
-  d3 f = disney_eval64(r, hd, dir);
+  d3 hv = env_value64(t, ev, iu, iv);
+  d3 f = disney_eval64(r, he, dir);
   return dvs(mul(scl(f, fabs(dot(dir, hd->normal))), hv), *pdf);
 }
 
 /* One sample (kernel.cu:369-443); returns the radiance before the clamp. */
 static d3 sample64(const orc64_scene* S, int32_t x, int32_t y, uint32_t idx, uint32_t sample, int32_t max_depth,
-                   uint32_t k0, uint32_t k1) {
+                   uint32_t k0, uint32_t k1, const eval64* ev) {
   const orc_scene* s = S->s;
   uint32_t q[4];
   double cu[5];
@@ -517,21 +555,23 @@ static d3 sample64(const orc64_scene* S, int32_t x, int32_t y, uint32_t idx, uin
   for (int32_t i = 0; i < max_depth; i++) {
     hit64 hit = closest(S, &ray);
     if (!hit.valid) {
-      double eu, ev;
-      spherical64(scl(ray.d, -1.0), &eu, &ev);
-      light = add(light, mul(tex_uv64(&s->env, eu, ev), red));
+      double eu, ev_;
+      spherical64(scl(ray.d, -1.0), &eu, &ev_);
+      light = add(light, mul(env_value64(&s->env, ev, eu, ev_), red));
       break;
     }
-    hd64 hd;
-    hit_data64(s, &s->mats[s->tri_mat[hit.id]], &hit, &hd);
+    hd64 hd, he;
+    const int32_t mid = s->tri_mat[hit.id];
+    hit_data64(s, &s->mats[mid], &hit, &hd);
+    hit_data_eval64(&s->mats[mid], mid, ev, &hd, &he);
     orc_philox(idx, sample, 2u + (uint32_t)i, 0, k0, k1, q);
     float r1 = orc_u01(q[3]);
     d3 dir = disney_sample64(&ray, &hd, orc_u01(q[0]), orc_u01(q[1]), orc_u01(q[2]));
-    d3 f = disney_eval64(&ray, &hd, dir);
+    d3 f = disney_eval64(&ray, &he, dir);
     double brdfPdf = disney_pdf64(&ray, &hd, dir);
     double hdriPdf, pointPdf = 0;
-    d3 hdriC = hdri_light64(S, &ray, hit.position, &hd, r1, &hdriPdf);
-    d3 pointC = point_light64(S, &ray, &hd, hit.position, &pointPdf, r1);
+    d3 hdriC = hdri_light64(S, &ray, hit.position, &hd, &he, ev, r1, &hdriPdf);
+    d3 pointC = point_light64(S, &ray, &hd, &he, hit.position, &pointPdf, r1);
     d3 brdfC = dvs(mul(scl(f, fabs(dot(dir, hd.normal))), hd.emission), brdfPdf);
     double den = hdriPdf + pointPdf + brdfPdf;
     d3 hl = mul(add(add(scl(hdriC, hdriPdf / den), scl(pointC, pointPdf / den)), scl(brdfC, brdfPdf / den)), red);
@@ -545,8 +585,11 @@ static d3 sample64(const orc64_scene* S, int32_t x, int32_t y, uint32_t idx, uin
 /* Mean over spp samples of the pixels with output indices idx[0..n):
  * rgb[3*i..] = mean of clamp(L, 0, 10) over non-NaN samples, counts[i] =
  * their number (kernel.cu:445-449). */
-void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
-                         int32_t max_depth, uint64_t seed, double* rgb, uint32_t* counts, int32_t nthreads) {
+void orc64_render_pixels_eval(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
+                              int32_t max_depth, uint64_t seed, const float* eval_mat, const float* eval_env,
+                              double* rgb, uint32_t* counts, int32_t nthreads) {
+  const eval64 evs = {eval_mat, eval_env};
+  const eval64* ev = (eval_mat || eval_env) ? &evs : NULL;
   const er_camera* c = &S->s->cam;
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
 #ifdef _OPENMP
@@ -559,7 +602,7 @@ void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, in
     double sx = 0, sy = 0, sz = 0;
     uint32_t cnt = 0;
     for (int32_t k = 0; k < spp; k++) {
-      d3 L = sample64(S, x, y, (uint32_t)o, (uint32_t)(sample_begin + k), max_depth, k0, k1);
+      d3 L = sample64(S, x, y, (uint32_t)o, (uint32_t)(sample_begin + k), max_depth, k0, k1, ev);
       double lx = clampd(L.x, 0, 10), ly = clampd(L.y, 0, 10), lz = clampd(L.z, 0, 10);
       if (lx != lx || ly != ly || lz != lz) continue;
       sx += lx; sy += ly; sz += lz;
@@ -570,6 +613,11 @@ void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, in
     rgb[3 * i + 2] = cnt ? sz / cnt : 0;
     counts[i] = cnt;
   }
+}
+
+void orc64_render_pixels(const orc64_scene* S, const int32_t* idx, int64_t n, int32_t spp, int32_t sample_begin,
+                         int32_t max_depth, uint64_t seed, double* rgb, uint32_t* counts, int32_t nthreads) {
+  orc64_render_pixels_eval(S, idx, n, spp, sample_begin, max_depth, seed, NULL, NULL, rgb, counts, nthreads);
 }
 
 /* Closest hit by this BVH for rays (n x 6: origin, direction; normalised

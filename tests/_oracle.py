@@ -58,6 +58,8 @@ def orc():
         _orc.orc64_render_pixels.argtypes = [C.c_void_p, A.IP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_uint64, C.POINTER(C.c_double), A.UP, C.c_int32]
         _orc.orc64_trace.argtypes = [C.c_void_p, A.FP, C.c_int64, A.IP, C.POINTER(C.c_double), C.c_int32]
+        _orc.orc64_render_pixels_eval.argtypes = [C.c_void_p, A.IP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                                  C.c_uint64, A.FP, A.FP, C.POINTER(C.c_double), A.UP, C.c_int32]
     return _orc
 
 
@@ -189,14 +191,19 @@ class Orc64:
     def __del__(self):
         self.close()
 
-    def render_pixels(self, idx, spp, max_depth, seed=0, sample_begin=0, nthreads=0):
+    def render_pixels(self, idx, spp, max_depth, seed=0, sample_begin=0, nthreads=0, eval_mat=None,
+                      eval_env=None):
         """Mean of clamp(L, 0, 10) over non-NaN samples for the pixels with
-        output indices idx: (rgb (n, 3) float64, counts (n,))."""
+        output indices idx: (rgb (n, 3) float64, counts (n,)).  eval_mat /
+        eval_env: evaluation parameters of the detached estimator."""
         idx = np.ascontiguousarray(idx, np.int32)
         rgb = np.zeros((len(idx), 3), np.float64)
         cnt = np.zeros(len(idx), np.uint32)
-        orc().orc64_render_pixels(self.h, _ptr(idx, A.IP), len(idx), spp, sample_begin, max_depth, seed,
-                                  rgb.ctypes.data_as(C.POINTER(C.c_double)), _ptr(cnt, A.UP), nthreads)
+        em = None if eval_mat is None else _f(eval_mat)
+        ee = None if eval_env is None else _f(eval_env)
+        orc().orc64_render_pixels_eval(self.h, _ptr(idx, A.IP), len(idx), spp, sample_begin, max_depth, seed,
+                                       None if em is None else _ptr(em), None if ee is None else _ptr(ee),
+                                       rgb.ctypes.data_as(C.POINTER(C.c_double)), _ptr(cnt, A.UP), nthreads)
         return rgb, cnt
 
     def trace(self, rays, nthreads=0):

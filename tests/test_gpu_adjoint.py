@@ -9,10 +9,13 @@
    checked parameter whose gradient is not negligible.
 3. The torch.autograd.Function returns the same gradients, and Adam steps
    on it lower the loss.
+4. The FP64 oracle's gradient (central differences of the same detached
+   estimator evaluated in double) agrees with the FP32 adjoint.
 """
 import numpy as np
 import pytest
 
+import _oracle as O
 from eleven import _abi as A
 from eleven import _lib, scenes
 
@@ -129,3 +132,47 @@ def test_torch_autograd_and_adam(small):
                                   lr=2e-2, spp=8, max_depth=DEPTH)
     assert hist[-1] < hist[0]
     s.set_params(m0, e0)
+
+
+def test_gradients_match_fp64_oracle(small):
+    """The GPU adjoint (FP32) against the FP64 oracle's gradient: central
+    differences (h = 1e-4) of the same detached estimator evaluated in
+    double (oracle/orc64.c), same samples.  Paths on which FP32 and FP64
+    round a discrete decision apart make the two estimators differ slightly,
+    so the bar is looser than the FP32 finite-difference check."""
+    arrays, s, T = small
+    m0, e0 = s.get_params()
+    out = s.render(SPP, max_depth=DEPTH, seed=SEED)
+    I0 = out["beauty"]
+    d = np.zeros_like(I0)
+    d[:, :3] = 2.0 * (I0[:, :3] - T[:, :3])
+    gm, ge, _ = s.backward(SPP, d, out["samples"], max_depth=DEPTH, seed=SEED)
+    orc = O.OrcScene(arrays)
+    o64 = O.Orc64(orc)
+    W, H = 48, 40
+    idx = np.arange(W * H)
+    T64 = T[:, :3].astype(np.float64)
+
+    def loss(m, e):
+        rgb, _ = o64.render_pixels(idx, SPP, DEPTH, seed=SEED, eval_mat=m, eval_env=e)
+        return float(((rgb - T64) ** 2).sum())
+
+    gmf, gef = gm.ravel(), ge.ravel()
+    picks = [("m", i) for i in np.argsort(-np.abs(gmf))[:6]] + [("e", i) for i in np.argsort(-np.abs(gef))[:6]]
+    h = 1e-4
+    errs = []
+    for kind, i in picks:
+        vals, xs = [], []
+        for sign in (1, -1):
+            m, e = m0.copy(), e0.copy()
+            (m if kind == "m" else e).ravel()[i] += sign * h
+            xs.append(float((m if kind == "m" else e).ravel()[i]))  # the float32 value actually used
+            vals.append(loss(m, e))
+        fd = (vals[0] - vals[1]) / (xs[0] - xs[1])
+        g = float(gmf[i] if kind == "m" else gef[i])
+        errs.append(abs(fd - g) / max(abs(fd), abs(g)))
+    print("\nadjoint vs FP64 oracle gradient, relative errors:", np.round(errs, 5))
+    assert np.median(errs) < 1e-2
+    assert max(errs) < 5e-2
+    o64.close()
+    orc.close()
