@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--bvh", default="fp32", choices=["fp32", "q8"])
     ap.add_argument("--max-leaf", type=int, default=0, help="triangles per BVH leaf (0 = library default)")
     ap.add_argument("--builder", default="host", choices=["host", "gpu"], help="BVH builder")
+    ap.add_argument("--env-sampling", default="search", choices=["search", "alias"],
+                    help="HDRI light sampling: the reference's CDF search or the alias table")
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -247,18 +249,24 @@ def run_gpu(args):
     b_ray_c = 32 + 16 + 32 * n_box_c + 36 * n_tri_c
     b_ray_s = 32 + 16 + 32 * n_box_s + 36 * n_tri_s
 
-    scene.render(spp=args.warmup, max_depth=max_depth, sample_begin=base + 1, flags=A.ER_RENDER_NO_OUTPUT)
+    env_flag = A.ER_RENDER_ENV_ALIAS if args.env_sampling == "alias" else 0
+    scene.render(spp=args.warmup, max_depth=max_depth, sample_begin=base + 1, flags=A.ER_RENDER_NO_OUTPUT | env_flag)
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.3)
     barrier(pg, local)
     t0 = time.perf_counter()
     st = scene.render(spp=args.steps, max_depth=max_depth, sample_begin=base + 1 + args.warmup,
-                      flags=A.ER_RENDER_NO_OUTPUT | A.ER_RENDER_PROFILE)["stats"]
+                      flags=A.ER_RENDER_NO_OUTPUT | env_flag)["stats"]
     wall = time.perf_counter() - t0
     ms = barrier_max(pg, local, st.ms)
     clk = clocks.stop()
     value = world * args.steps * npix / ms / 1e3
+    # per-kernel times: a profiled pass (events after every launch, waves on
+    # one stream) of the same samples
+    prof_steps = min(args.steps, 8)
+    pst = scene.render(spp=prof_steps, max_depth=max_depth, sample_begin=base + 1 + args.warmup,
+                       flags=A.ER_RENDER_NO_OUTPUT | A.ER_RENDER_PROFILE | env_flag)["stats"]
 
     # e2e through the C-ABI with host buffers, one 1-spp call per step
     beauty = np.zeros((npix, 4), np.float32)
@@ -271,7 +279,7 @@ def run_gpu(args):
     t0 = time.perf_counter()
     for i in range(args.e2e_steps):
         o.sample_begin = base + 2 + args.warmup + args.steps + i
-        o.flags = A.ER_RENDER_CONTINUE if i else 0
+        o.flags = (A.ER_RENDER_CONTINUE if i else 0) | env_flag
         _lib.check(L.er_render(scene.h, C.byref(o), beauty.ctypes.data_as(C.c_void_p), None, None, None,
                                samples.ctypes.data_as(C.c_void_p), pathcount.ctypes.data_as(C.c_void_p), None),
                    "er_render")
@@ -280,9 +288,9 @@ def run_gpu(args):
     d2h = beauty.nbytes + samples.nbytes + pathcount.nbytes
 
     # roofline of the dominant kernel: k_trace (extension + shadow rays)
-    kname, kms, nl = "k_trace", st.stage_ms[1], st.stage_launches[1]
-    rays = st.rays_closest + st.rays_shadow
-    alg_bytes = st.rays_closest * b_ray_c + st.rays_shadow * b_ray_s
+    kname, kms, nl = "k_trace", pst.stage_ms[1], pst.stage_launches[1]
+    rays = pst.rays_closest + pst.rays_shadow
+    alg_bytes = pst.rays_closest * b_ray_c + pst.rays_shadow * b_ray_s
     b_ray = alg_bytes / max(rays, 1)
     peak, peak_src = peaks()
     achieved = alg_bytes / (kms * 1e-3) / 1e9
@@ -290,7 +298,7 @@ def run_gpu(args):
     traffic = None
     if tr and tr.get("kernel") == kname and args.config == tr.get("config"):
         traffic = tr["dram_bytes_per_ray"] * rays / max(nl, 1)
-    stage = {n: round(st.stage_ms[k] / args.steps, 3) for k, n in enumerate(A.STAGES)}
+    stage = {n: round(pst.stage_ms[k] / prof_steps, 3) for k, n in enumerate(A.STAGES)}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -298,6 +306,7 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, reference scene shapes)",
         "config": dict(cfg, spp_per_step=1, bvh=args.bvh, max_leaf_tris=args.max_leaf or 4, bvh_builder=args.builder,
+                       env_sampling=args.env_sampling,
                        triangles=arrays.tri_count,
                        l2="working set > 126 MB L2 (no flush)", parallelism="replicas" if world > 1 else "1 GPU"),
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(C.sizeof(A.er_render_opts)),
@@ -306,11 +315,13 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "algorithmic_bytes_per_ray": round(b_ray, 1),
-                     "launches": int(nl), "avg_launch_ms": round(kms / max(nl, 1), 4)},
+                     "launches": int(nl), "avg_launch_ms": round(kms / max(nl, 1), 4),
+                     "timing": f"CUDA events after every launch, profiled pass of {prof_steps} steps on one stream"},
         "rays_per_s": {"closest": round(st.rays_closest / ms / 1e3, 1), "shadow": round(st.rays_shadow / ms / 1e3, 1),
                        "unit": "Mrays/s"},
         "path_vertices_per_s": round(st.path_vertices / ms / 1e3, 1),
         "stage_ms_per_step": stage,
+        "profiled_ms_per_step": round(pst.ms / prof_steps, 4),
         "per_ray": {"closest_box_tests": round(n_box_c, 2), "closest_tri_tests": round(n_tri_c, 2),
                     "shadow_box_tests": round(n_box_s, 2), "shadow_tri_tests": round(n_tri_s, 2)},
         "scene": {"bvh_build_ms": round(info.bvh_build_ms, 1), "upload_ms": round(info.upload_ms, 1),

@@ -189,8 +189,15 @@ enum {
   ER_RENDER_NO_OUTPUT = 1u << 5,  /* render into the film only              */
   ER_RENDER_PROFILE = 1u << 6,    /* CUDA-event time per stage (stats)      */
   ER_RENDER_COUNT = 1u << 7,      /* count node visits / triangle tests     */
-  ER_RENDER_SNAPSHOTS = 1u << 8   /* copy the film to the snapshot buffer
+  ER_RENDER_SNAPSHOTS = 1u << 8,  /* copy the film to the snapshot buffer
                                      after every wave (er_snapshot)         */
+  ER_RENDER_ONE_STREAM = 1u << 9  /* run the waves one after another on the
+                                     scene's stream.  Default with two or
+                                     more waves: two waves in flight on two
+                                     streams (the second an internal one),
+                                     accumulated in sample order, so the
+                                     film is the same; ER_RENDER_PROFILE
+                                     implies this flag                      */
 };
 
 /* Stages of the wavefront, indices of er_render_stats.stage_ms.  TRACE is

@@ -30,6 +30,20 @@ def test_header_and_exports_agree():
         assert hasattr(L, name), name
 
 
+def test_flag_constants_agree():
+    """Every `ER_X = 1u << n` / `ER_X = n` enum constant of the header has
+    the same value in the ctypes mirror."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    found = 0
+    for name, shift, val in re.findall(r"\b(ER_[A-Z0-9_]+)\s*=\s*(?:1u?\s*<<\s*(\d+)|(\d+))\s*[,}\n]", src):
+        if not hasattr(A, name):
+            continue
+        want = (1 << int(shift)) if shift else int(val)
+        assert getattr(A, name) == want, name
+        found += 1
+    assert found >= 12
+
+
 def test_library_exports_in_symbol_table():
     out = subprocess.run(["nm", "-D", "--defined-only", _lib.lib_path()], capture_output=True, text=True).stdout
     syms = {l.split()[-1] for l in out.splitlines() if l.strip()}

@@ -133,10 +133,19 @@ def test_continue_equals_single_call(c0):
 
 
 def test_wave_split_is_deterministic(c0):
+    """One wave, several waves on two streams (the default with more than
+    one wave), and several waves on one stream give the same film."""
     arrays, scene, orc = c0
     a = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=4)["beauty"]
     b = scene.render(spp=4, max_depth=4, seed=2, spp_per_wave=1)["beauty"]
     assert np.array_equal(a, b)
+    for sw in (1, 2, 3):
+        two = scene.render(spp=7, max_depth=4, seed=5, spp_per_wave=sw, aov=True)
+        one = scene.render(spp=7, max_depth=4, seed=5, spp_per_wave=sw, aov=True, flags=A.ER_RENDER_ONE_STREAM)
+        for k in ("beauty", "normal", "tangent", "bitangent", "samples", "pathcount"):
+            assert np.array_equal(two[k], one[k]), (sw, k)
+    c = scene.render(spp=7, max_depth=4, seed=5, spp_per_wave=7)["beauty"]
+    assert np.array_equal(c, two["beauty"])
 
 
 def test_normal_map_paths_match_oracle():

@@ -223,6 +223,11 @@ struct er_scene {
   int num_sms = 0;
   er::Film film;
   er::Wave* wave = nullptr;
+  // second wave in flight (its own buffers and stream), so that one wave's
+  // launches fill the other's traversal tails
+  er::Wave* wave2 = nullptr;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_acc[2] = {nullptr, nullptr};
   uint32_t* err_word = nullptr;   // device error word (bounds / timeout)
   unsigned long long* d_stats = nullptr;  // device ray counters
   std::vector<cudaEvent_t> ev_pool;       // per-launch profiling events

@@ -601,6 +601,31 @@ er_status ensure_wave(er_scene* s, int64_t cap, bool aov, bool grad = false) {
   return st;
 }
 
+// The second wave of the two-stream schedule, its stream and events; the
+// same capacity and passes as the first.
+er_status ensure_wave2(er_scene* s) {
+  const Wave* w1 = s->wave;
+  if (!s->wave2 || s->wave2->cap < w1->cap || (w1->v.aov && !s->wave2->v.aov)) {
+    if (s->wave2) {
+      for (void* p : s->wave2->mem) cudaFree(p);
+      delete s->wave2;
+    }
+    s->wave2 = new Wave();
+    er_status st = wave_fill(s->wave2, w1->cap, w1->v.aov, false, s->d_stats);
+    if (st != ER_OK) {
+      for (void* p : s->wave2->mem) cudaFree(p);
+      delete s->wave2;
+      s->wave2 = nullptr;
+      return st;
+    }
+  }
+  if (!s->stream2) ER_CUDA(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
+  if (!s->ev_fork) ER_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+  for (cudaEvent_t& e : s->ev_acc)
+    if (!e) ER_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return ER_OK;
+}
+
 er_status ensure_film(er_scene* s, bool aov, bool fp64, bool clear) {
   Film& F = s->film;
   int32_t W = s->camera.x_res, H = s->camera.y_res;
@@ -655,7 +680,6 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   if (dump_rad) sw = o->spp;
   er_status st = ensure_wave(s, (int64_t)sw * npix, aov);
   if (st != ER_OK) return st;
-  WaveView& w = s->wave->v;
   WaveParams P;
   P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
   P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
@@ -663,6 +687,15 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   const bool q8 = s->dev.use_q8;
   const bool count = o->flags & ER_RENDER_COUNT;
   const bool prof = o->flags & ER_RENDER_PROFILE;
+  // Two waves in flight: wave k runs on stream k % 2 with its own buffers;
+  // accumulate(k) waits for accumulate(k - 1), so the film sees the samples
+  // in index order as with one stream.
+  const bool two = !dump_rad && !prof && !(o->flags & ER_RENDER_ONE_STREAM) && o->spp > sw;
+  if (two) {
+    if ((st = ensure_wave2(s)) != ER_OK) return st;
+    ER_CUDA(cudaEventRecord(s->ev_fork, s->stream));
+    ER_CUDA(cudaStreamWaitEvent(s->stream2, s->ev_fork, 0));
+  }
   static int g_tr[4] = {0}, g_shade = 0;
   if (!g_shade) {
     g_tr[0] = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
@@ -697,47 +730,55 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     }
     ER_CUDA(cudaEventRecord(s->ev_pool[0], s->stream));
   }
-  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+  int32_t k = 0;
+  for (int32_t s0 = 0; s0 < o->spp; s0 += sw, k++) {
+    const bool alt = two && (k & 1);
+    WaveView& w = alt ? s->wave2->v : s->wave->v;
+    cudaStream_t strm = alt ? s->stream2 : s->stream;
     int32_t cur = std::min(sw, o->spp - s0);
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     int32_t n = cur * npix;
-    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, GradArgs{});
+    k_raygen<false><<<(n + 255) / 256, 256, 0, strm>>>(s->dev, w, P, n, NB, GradArgs{});
     if ((st = mark(ER_STAGE_RAYGEN)) != ER_OK) return st;
     // trace(b): extension rays of bounce b + shadow rays of bounce b-1;
     // the extra trace(max_depth) finishes the last bounce's shadow rays.
     for (int32_t b = 0; b <= max_depth; b++) {
       uint32_t* err = s->err_word;
       switch (variant) {
-        case 0: k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
-        case 1: k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
-        case 2: k_trace<false, true, false><<<g_tr[2], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
-        default: k_trace<true, true, false><<<g_tr[3], kTravBlock, 0, s->stream>>>(s->dev, w, b, err, NB, 7u); break;
+        case 0: k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, strm>>>(s->dev, w, b, err, NB, 7u); break;
+        case 1: k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, strm>>>(s->dev, w, b, err, NB, 7u); break;
+        case 2: k_trace<false, true, false><<<g_tr[2], kTravBlock, 0, strm>>>(s->dev, w, b, err, NB, 7u); break;
+        default: k_trace<true, true, false><<<g_tr[3], kTravBlock, 0, strm>>>(s->dev, w, b, err, NB, 7u); break;
       }
       if ((st = mark(ER_STAGE_TRACE)) != ER_OK) return st;
       if (b == max_depth) break;
-      k_shade<false><<<g_shade, 128, 0, s->stream>>>(s->dev, w, P, b, NB, GradArgs{});
+      k_shade<false><<<g_shade, 128, 0, strm>>>(s->dev, w, P, b, NB, GradArgs{});
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
     }
     if (dump_rad) {
       k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, dump_rad, dump_b);
     } else {
       Film F = s->film;
-      k_accumulate<false><<<(npix + 127) / 128, 128, 0, s->stream>>>(w, P, F, cur, NB);
+      if (two && k > 0) ER_CUDA(cudaStreamWaitEvent(strm, s->ev_acc[(k - 1) & 1], 0));
+      k_accumulate<false><<<(npix + 127) / 128, 128, 0, strm>>>(w, P, F, cur, NB);
       if (o->flags & ER_RENDER_SNAPSHOTS) {
         // the reader (er_snapshot) holds the lock while it copies the
         // snapshot out, so the buffer is not overwritten under it
         std::lock_guard<std::mutex> lk(s->snap_mu);
         ER_CUDA(cudaMemcpyAsync(s->snap_beauty, F.beauty, (size_t)npix * sizeof(float4), cudaMemcpyDeviceToDevice,
-                                s->stream));
-        ER_CUDA(cudaMemcpyAsync(s->snap_samples, F.samples, (size_t)npix * 4, cudaMemcpyDeviceToDevice, s->stream));
-        ER_CUDA(cudaEventRecord(s->snap_event, s->stream));
+                                strm));
+        ER_CUDA(cudaMemcpyAsync(s->snap_samples, F.samples, (size_t)npix * 4, cudaMemcpyDeviceToDevice, strm));
+        ER_CUDA(cudaEventRecord(s->snap_event, strm));
         s->snap_valid = true;
       }
+      if (two) ER_CUDA(cudaEventRecord(s->ev_acc[k & 1], strm));
     }
     if ((st = mark(ER_STAGE_ACCUMULATE)) != ER_OK) return st;
     ER_CUDA(cudaGetLastError());
   }
+  // join: the last accumulate follows every launch of both streams
+  if (two) ER_CUDA(cudaStreamWaitEvent(s->stream, s->ev_acc[(k - 1) & 1], 0));
   if (launches) *launches = nl;
   return ER_OK;
 }
@@ -776,10 +817,12 @@ er_status check_opts(er_scene* s, const er_render_opts* o) {
 }  // namespace
 
 void free_wave(er_scene* s) {
-  if (!s->wave) return;
-  for (void* p : s->wave->mem) cudaFree(p);
-  delete s->wave;
-  s->wave = nullptr;
+  for (Wave** pw : {&s->wave, &s->wave2}) {
+    if (!*pw) continue;
+    for (void* p : (*pw)->mem) cudaFree(p);
+    delete *pw;
+    *pw = nullptr;
+  }
 }
 
 void free_film(er_scene* s) {

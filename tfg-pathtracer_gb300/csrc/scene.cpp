@@ -429,6 +429,10 @@ extern "C" er_status er_scene_free(er_scene* s) {
   cudaFree(s->snap_samples);
   if (s->snap_event) cudaEventDestroy(s->snap_event);
   if (s->snap_stream) cudaStreamDestroy(s->snap_stream);
+  if (s->stream2) cudaStreamDestroy(s->stream2);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  for (cudaEvent_t e : s->ev_acc)
+    if (e) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return ER_OK;

@@ -130,6 +130,7 @@ class er_render_opts(C.Structure):
 ER_RENDER_PROFILE = 1 << 6
 ER_RENDER_COUNT = 1 << 7
 ER_RENDER_SNAPSHOTS = 1 << 8
+ER_RENDER_ONE_STREAM = 1 << 9
 STAGES = ["raygen", "trace", "shade", "reserved", "accumulate"]
 
 
