@@ -209,10 +209,9 @@ er_status build_bvh4(const er_scene_desc* d, int max_leaf, BuildResult* out) {
   }
   if (T == 0) {
     out->nodes.assign(32, 0.0f);
-    for (int s = 0; s < 4; s++) {
-      int32_t e = kEmpty;
-      std::memcpy(&out->nodes[24 + s], &e, 4);
-    }
+    Box z;
+    z.reset();  // inverted: lo = +inf, hi = -inf
+    for (int s = 0; s < 4; s++) put_child(out->nodes.data(), s, z, kEmpty, 0.0f);
     out->node_count = 1;
     out->leaf_count = 0;
     out->depth = 1;
@@ -267,7 +266,7 @@ er_status build_bvh4(const er_scene_desc* d, int max_leaf, BuildResult* out) {
         maxd = std::max(maxd, c.delta);
       } else {
         Box z;
-        for (int k = 0; k < 3; k++) { z.lo[k] = 0; z.hi[k] = 0; }
+        z.reset();  // inverted: lo = +inf, hi = -inf
         put_child(nd, s, z, kEmpty, 0.0f);
       }
     }

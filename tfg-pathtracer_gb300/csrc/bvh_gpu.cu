@@ -238,7 +238,8 @@ __global__ void k_collapse(const BNode* nodes, const float* pos, const int32_t* 
   float* nd = out_nodes + 32 * (int64_t)I.out;
   for (int s = 0; s < 4; s++) {
     int32_t ref = kEmpty;
-    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}, dl = 0.f;
+    // an empty slot keeps an inverted box (lo = +inf, hi = -inf)
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, dl = 0.f;
     if (s < nc) {
       int32_t cnt, first;
       child_info(nodes, pos, sorted, tdelta, ch[s], lo, hi, &dl, &cnt, &first);
@@ -396,6 +397,11 @@ er_status build_bvh_gpu(er_scene* s, const er_scene_desc* d, int max_leaf, const
     for (int sl = 0; sl < 4; sl++) {
       int32_t r = sl == 0 ? ref : kEmpty;
       std::memcpy(&root[24 + sl], &r, 4);
+      if (r == kEmpty)
+        for (int k = 0; k < 3; k++) {
+          root[4 * 2 * k + sl] = INFINITY;         // inverted box of an empty slot
+          root[4 * (2 * k + 1) + sl] = -INFINITY;
+        }
     }
     if (n > 0) {
       for (int k = 0; k < 3; k++) { root[4 * 2 * k] = lo[k]; root[4 * (2 * k + 1)] = hi[k]; }

@@ -31,6 +31,8 @@ er_status cuda_fail(cudaError_t e, const char* what);
 //   [6] child[4] (int bits)  [7] shading-offset bound of each child (float)
 // child: >= 0 internal node index; kEmpty = no child; otherwise a leaf:
 //   bit 31 set, bits 30..27 = tri count - 1, bits 26..0 = first leaf slot.
+// An empty slot's box is inverted, lo = +inf and hi = -inf on every axis,
+// so the slab test rejects it for every ray without looking at the child.
 constexpr int32_t kEmpty = -1;
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kLeafCountShift = 27;

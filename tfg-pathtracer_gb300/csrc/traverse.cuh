@@ -227,7 +227,7 @@ struct Traverser {
   }
 
   // Expands `node`: tests its four child boxes, postpones / pushes leaf
-  // children, pushes the farther internal children and continues with the
+  // children, pushes the other internal children and continues with the
   // nearest.
   __device__ __forceinline__ void node_step(const DevScene& S, int2* sstk, int2* lstk, TravStats& st, uint32_t* err) {
     if (--guard < 0 || (uint64_t)node >= (uint64_t)S.n_nodes) {
@@ -277,7 +277,10 @@ struct Traverser {
     for (int c = 0; c < 4; c++) {
       float tnear = max3f(fmaf(nxa[c], inv.x, bnear.x), fmaf(nya[c], inv.y, bnear.y), fmaf(nza[c], inv.z, bnear.z));
       float tfar = min3f(fmaf(fxa[c], inv.x, bfar.x), fmaf(fya[c], inv.y, bfar.y), fmaf(fza[c], inv.z, bfar.z));
-      bool hit = cha[c] != kEmpty && tnear <= tfar && tfar >= -slack;
+      // FP32 nodes reject empty slots by their inverted boxes; a Q8 empty
+      // slot decodes to an inverted box too, but the bias widening could
+      // reopen it on a tiny node, so it is checked
+      bool hit = (!Q8 || cha[c] != kEmpty) && tnear <= tfar && tfar >= -slack;
       float key = MODE == kAny ? tnear : tnear - dla[c];
       if (MODE != kAny) hit = hit && key <= lim;
       bool is_leaf = cha[c] < 0;
@@ -292,25 +295,19 @@ struct Traverser {
       ik[c] = hit && !is_leaf ? key : INFINITY;
       ic[c] = cha[c];
     }
-    // internal children: nearest first
-    float k0 = ik[0], k1 = ik[1], k2 = ik[2], k3 = ik[3];
-    int32_t c0 = ic[0], c1 = ic[1], c2 = ic[2], c3 = ic[3];
-#define ER_CSWAP(ka, ca, kb, cb)                         \
-  if (kb < ka) {                                         \
-    float tk = ka; ka = kb; kb = tk;                     \
-    int32_t tc = ca; ca = cb; cb = tc;                   \
-  }
-    ER_CSWAP(k0, c0, k1, c1);
-    ER_CSWAP(k2, c2, k3, c3);
-    ER_CSWAP(k0, c0, k2, c2);
-    ER_CSWAP(k1, c1, k3, c3);
-    ER_CSWAP(k1, c1, k2, c2);
-#undef ER_CSWAP
-    if (k3 < INFINITY && !push(sstk, lstk, c3, k3, err)) return;
-    if (k2 < INFINITY && !push(sstk, lstk, c2, k2, err)) return;
-    if (k1 < INFINITY && !push(sstk, lstk, c1, k1, err)) return;
-    if (k0 < INFINITY) {
-      node = c0;
+    // internal children: the nearest is expanded next, the others are
+    // pushed in slot order (their keys still prune them at the pop; a full
+    // sort cost more than it saved: 2 % slower on the 1080p scene)
+    float kmin = ik[0];
+    int im = 0;
+#pragma unroll
+    for (int c = 1; c < 4; c++)
+      if (ik[c] < kmin) { kmin = ik[c]; im = c; }
+#pragma unroll
+    for (int c = 3; c >= 0; c--)
+      if (c != im && ik[c] < INFINITY && !push(sstk, lstk, ic[c], ik[c], err)) return;
+    if (kmin < INFINITY) {
+      node = ic[im];
       return;
     }
     pop_next(sstk, lstk, err);
