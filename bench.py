@@ -410,7 +410,7 @@ def run_batch(args):
                     "gpu_launches": int(stats[-1].kernel_launches), "waves": n_waves,
                     "tuning": {"wave_paths": tuning.wave_paths, "trace_blocks_per_sm": tuning.trace_blocks_per_sm,
                                "shade_blocks_per_sm": tuning.shade_blocks_per_sm,
-                               "split_trace": tuning.split_trace},
+                               "split_trace": tuning.split_trace, "one_stream": tuning.one_stream},
                     "autotune_s": round(t_tune, 1), "device_bytes": batch_bytes},
         "speedup_batched_vs_plain": round(pm / bm, 3),
         "films_bit_identical": same,

@@ -378,7 +378,8 @@ typedef struct er_batch_tuning {
   int32_t shade_blocks_per_sm;  /* shading grid = SMs x this; 0 = as many as fit */
   int32_t split_trace;          /* 1: extension, point-light and env rays as three traversal launches */
   int32_t use_graph;            /* 1: capture the launch sequence once and replay it */
-  int32_t reserved[3];
+  int32_t one_stream;           /* 1: waves one after another; 0: two waves in flight on two streams */
+  int32_t reserved[2];
 } er_batch_tuning;
 
 /* opts: bvh_format (ER_BVH_Q8 needs scenes built with it) and stream. */

@@ -68,16 +68,18 @@ def _check(batch, singles):
         assert np.array_equal(got["pathcount"], pc), f"job {k} pathcount"
 
 
-def _tuning(wave_paths=0, trace=0, shade=0, split=0, graph=1):
+def _tuning(wave_paths=0, trace=0, shade=0, split=0, graph=1, one_stream=0):
     t = A.er_batch_tuning()
     t.wave_paths, t.trace_blocks_per_sm, t.shade_blocks_per_sm = wave_paths, trace, shade
-    t.split_trace, t.use_graph = split, graph
+    t.split_trace, t.use_graph, t.one_stream = split, graph, one_stream
     return t
 
 
 @pytest.mark.parametrize("tuning", [
     dict(),                                       # defaults: one wave, graph
-    dict(wave_paths=9000, graph=0),               # many waves, jobs in slices, direct launches
+    dict(wave_paths=9000, graph=0),               # many waves on two streams, jobs in slices, direct launches
+    dict(wave_paths=9000),                        # the same captured in a graph (fork / join in the capture)
+    dict(wave_paths=9000, one_stream=1),          # many waves on one stream
     dict(wave_paths=12000, split=1, trace=3, shade=2),
 ])
 def test_batch_equals_single_renders(world, singles, tuning):

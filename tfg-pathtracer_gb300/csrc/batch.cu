@@ -52,6 +52,7 @@ struct er_batch {
   BatchSeg* d_segs = nullptr;
   Wave* wave = nullptr;
   int64_t wave_cap = 0;
+  BatchPair pair;  // second wave pipeline (allocated on first use)
   // captured launch sequence
   cudaGraphExec_t graph = nullptr;
   er_batch_tuning graph_tuning{};
@@ -243,7 +244,9 @@ er_status make_plan(er_batch* b, int64_t budget) {
   if (!b->wave || b->wave_cap < cap) {
     drop_graph(b);
     wave_destroy(b->wave);
+    wave_destroy(b->pair.w2);
     b->wave = nullptr;
+    b->pair.w2 = nullptr;
     b->wave_cap = 0;
     er_status st = wave_create(std::max<int64_t>(cap, 1), b->d_stats, &b->wave);
     if (st != ER_OK) return st;
@@ -262,7 +265,22 @@ er_batch_tuning default_tuning() {
 
 bool same_tuning(const er_batch_tuning& a, const er_batch_tuning& b) {
   return a.wave_paths == b.wave_paths && a.trace_blocks_per_sm == b.trace_blocks_per_sm &&
-         a.shade_blocks_per_sm == b.shade_blocks_per_sm && a.split_trace == b.split_trace;
+         a.shade_blocks_per_sm == b.shade_blocks_per_sm && a.split_trace == b.split_trace &&
+         a.one_stream == b.one_stream;
+}
+
+// The second pipeline's buffers (the first's capacity), stream and events.
+er_status ensure_pair(er_batch* b) {
+  BatchPair& p = b->pair;
+  if (!p.w2) {
+    drop_graph(b);
+    er_status st = wave_create(std::max<int64_t>(b->wave_cap, 1), b->d_stats, &p.w2);
+    if (st != ER_OK) return st;
+  }
+  if (!p.s2) ER_CUDA(cudaStreamCreateWithFlags(&p.s2, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&p.ev_fork, &p.ev_join, &p.ev_acc[0], &p.ev_acc[1]})
+    if (!*e) ER_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  return ER_OK;
 }
 
 int32_t max_job_npix(const er_batch* b) {
@@ -288,8 +306,13 @@ er_status enqueue_render(er_batch* b, const er_batch_tuning& t, int64_t* launche
   sch.shade_blocks_per_sm = t.shade_blocks_per_sm;
   sch.split_trace = t.split_trace != 0;
   int64_t nl = 0;
+  const BatchPair* pair = nullptr;
+  if (!t.one_stream && b->waves.size() >= 2) {
+    if (!b->pair.w2) return fail(ER_ERR_INVALID_ARG, "second wave pipeline missing");
+    pair = &b->pair;
+  }
   er_status st = batch_launch(b->dev, b->wave, b->d_segs, b->d_jobs, b->waves, sch, b->num_sms, b->err_word,
-                              b->stream, &nl);
+                              b->stream, &nl, pair);
   if (launches) *launches = nl + (int64_t)b->films.size();
   return st;
 }
@@ -298,6 +321,8 @@ er_status enqueue_render(er_batch* b, const er_batch_tuning& t, int64_t* launche
 er_status render_once(er_batch* b, const er_batch_tuning& t, double* ms, int64_t* launches) {
   er_status st = make_plan(b, wave_budget(b, t));
   if (st != ER_OK) return st;
+  // (allocations happen here, outside any stream capture)
+  if (!t.one_stream && b->waves.size() >= 2 && (st = ensure_pair(b)) != ER_OK) return st;
   int64_t nl = 0;
   if (t.use_graph) {
     if (!b->graph || !same_tuning(b->graph_tuning, t)) {
@@ -636,6 +661,7 @@ extern "C" er_status er_batch_autotune(er_batch* b, int32_t reps, er_batch_tunin
   if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.shade_blocks_per_sm = v; }, {0, 4, 8})) != ER_OK)
     return st;
   if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.split_trace = v; }, {0, 1})) != ER_OK) return st;
+  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.one_stream = v; }, {0, 1})) != ER_OK) return st;
   b->tuned = cur;
   b->has_tuned = true;
   if (best) *best = cur;
@@ -654,8 +680,13 @@ extern "C" er_status er_batch_free(er_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
+  if (b->pair.s2) cudaStreamSynchronize(b->pair.s2);
   wave_destroy(b->wave);
+  wave_destroy(b->pair.w2);
   for (void* p : b->allocs) cudaFree(p);
+  if (b->pair.s2) cudaStreamDestroy(b->pair.s2);
+  for (cudaEvent_t e : {b->pair.ev_fork, b->pair.ev_join, b->pair.ev_acc[0], b->pair.ev_acc[1]})
+    if (e) cudaEventDestroy(e);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);

@@ -211,6 +211,14 @@ struct BatchSchedule {
   bool split_trace;             // extension / point / env traversal as three launches
 };
 
+// Second wave pipeline of a batch: waves alternate between (wave, stream)
+// and (w2, s2); accumulates are chained by ev_acc in wave order.
+struct BatchPair {
+  Wave* w2 = nullptr;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_acc[2] = {nullptr, nullptr};
+};
+
 }  // namespace er
 
 struct er_scene {
@@ -287,5 +295,5 @@ er_status film_clear(const Film& F, cudaStream_t stream);
 // Launches every wave of a batch plan on `stream` (render.cu).
 er_status batch_launch(const DevScene& S, Wave* w, const BatchSeg* d_segs, const BatchJobDev* d_jobs,
                        const std::vector<BatchWave>& waves, const BatchSchedule& sch, int num_sms, uint32_t* err,
-                       cudaStream_t stream, int64_t* launches);
+                       cudaStream_t stream, int64_t* launches, const BatchPair* pair = nullptr);
 }  // namespace er

@@ -304,9 +304,18 @@ __device__ __forceinline__ void grad_prev_vertex(const DevScene& S, const WavePa
                   G.g_mat, G.g_env);
 }
 
+#ifndef ER_SHADE_MIN_BLOCKS
+#define ER_SHADE_MIN_BLOCKS 6
+#endif
+// Resident 128-thread shade blocks per SM the register budget is sized for
+// (85 registers; unbounded the kernel takes 117 and 4 blocks, and the
+// latency of its texture / CDF loads is poorly hidden: 10 % longer on the
+// 1080p scene).  The gradient variant keeps its full budget.
+constexpr int kShadeMinBlocks = ER_SHADE_MIN_BLOCKS;
+
 template <bool BATCH, bool GRAD = false>
-__global__ void __launch_bounds__(128) k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B,
-                                               GradArgs G) {
+__global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
+    k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B, GradArgs G) {
   const int32_t qin = bounce & 1;
   const int32_t n = w.counts[kExt + qin];
   const float4* qo = w.q_o[qin];
@@ -915,7 +924,7 @@ er_status film_clear(const Film& F, cudaStream_t stream) {
 // sample order, so each job's film equals a single-scene render's.
 er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, const BatchJobDev* d_jobs,
                        const std::vector<BatchWave>& waves, const BatchSchedule& sch, int num_sms, uint32_t* err,
-                       cudaStream_t stream, int64_t* launches) {
+                       cudaStream_t stream, int64_t* launches, const BatchPair* pair) {
   static int occ_tr[2] = {0, 0}, occ_sh = 0;  // resident blocks per SM
   if (!occ_sh) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tr[0], k_trace<false, false, true>, kTravBlock, 0);
@@ -931,23 +940,33 @@ er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, cons
   const int g_tr = tb * num_sms, g_sh = sb * num_sms;
   if (launches) *launches = 0;
   if (waves.empty()) return ER_OK;  // (also: occupancy queries done before any stream capture)
-  const WaveView& w = wv->v;
   const WaveParams P0{};
   int64_t nl = 0;
-  auto trace = [&](int32_t b, const BatchView& B, uint32_t phases) {
-    if (q8) k_trace<true, false, true><<<g_tr, kTravBlock, 0, stream>>>(S, w, b, err, B, phases);
-    else k_trace<false, false, true><<<g_tr, kTravBlock, 0, stream>>>(S, w, b, err, B, phases);
-    nl++;
-  };
-  for (const BatchWave& bw : waves) {
-    if (bw.n_paths > wv->cap) return fail(ER_ERR_INVALID_ARG, "batch wave larger than its buffers");
+  // two pipelines: wave k on (pair->w2, pair->s2) when k is odd
+  const bool two = pair && pair->w2 && waves.size() >= 2;
+  if (two) {
+    ER_CUDA(cudaEventRecord(pair->ev_fork, stream));
+    ER_CUDA(cudaStreamWaitEvent(pair->s2, pair->ev_fork, 0));
+  }
+  for (size_t k = 0; k < waves.size(); k++) {
+    const BatchWave& bw = waves[k];
+    const bool alt = two && (k & 1);
+    const Wave* wk = alt ? pair->w2 : wv;
+    const WaveView& w = wk->v;
+    cudaStream_t strm = alt ? pair->s2 : stream;
+    auto trace = [&](int32_t b, const BatchView& B, uint32_t phases) {
+      if (q8) k_trace<true, false, true><<<g_tr, kTravBlock, 0, strm>>>(S, w, b, err, B, phases);
+      else k_trace<false, false, true><<<g_tr, kTravBlock, 0, strm>>>(S, w, b, err, B, phases);
+      nl++;
+    };
+    if (bw.n_paths > wk->cap) return fail(ER_ERR_INVALID_ARG, "batch wave larger than its buffers");
     BatchView B;
     B.segs = d_segs + bw.seg_begin;
     B.jobs = d_jobs;
     B.n_segs = bw.n_segs;
     B.n_acc = bw.n_acc;
     const int32_t n = bw.n_paths;
-    k_raygen<true><<<(n + 255) / 256, 256, 0, stream>>>(S, w, P0, n, B, GradArgs{});
+    k_raygen<true><<<(n + 255) / 256, 256, 0, strm>>>(S, w, P0, n, B, GradArgs{});
     nl++;
     for (int32_t b = 0; b <= bw.max_depth; b++) {
       if (sch.split_trace) {
@@ -958,11 +977,19 @@ er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, cons
         trace(b, B, 7u);
       }
       if (b == bw.max_depth) break;
-      k_shade<true><<<g_sh, 128, 0, stream>>>(S, w, P0, b, B, GradArgs{});
+      k_shade<true><<<g_sh, 128, 0, strm>>>(S, w, P0, b, B, GradArgs{});
       nl++;
     }
-    k_accumulate<true><<<(bw.n_acc + 127) / 128, 128, 0, stream>>>(w, P0, Film(), 0, B);
+    // a job's slices accumulate in wave order
+    if (two && k > 0) ER_CUDA(cudaStreamWaitEvent(strm, pair->ev_acc[(k - 1) & 1], 0));
+    k_accumulate<true><<<(bw.n_acc + 127) / 128, 128, 0, strm>>>(w, P0, Film(), 0, B);
     nl++;
+    if (two) ER_CUDA(cudaEventRecord(pair->ev_acc[k & 1], strm));
+  }
+  if (two) {
+    ER_CUDA(cudaEventRecord(pair->ev_join, pair->s2));
+    ER_CUDA(cudaStreamWaitEvent(stream, pair->ev_join, 0));
+    ER_CUDA(cudaStreamWaitEvent(stream, pair->ev_acc[(waves.size() - 1) & 1], 0));
   }
   ER_CUDA(cudaGetLastError());
   if (launches) *launches = nl;

@@ -164,7 +164,7 @@ class er_batch_tuning(C.Structure):
     _fields_ = [
         ("wave_paths", C.c_int32), ("trace_blocks_per_sm", C.c_int32),
         ("shade_blocks_per_sm", C.c_int32), ("split_trace", C.c_int32),
-        ("use_graph", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("use_graph", C.c_int32), ("one_stream", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 

@@ -27,7 +27,12 @@ REF_SRC = os.environ.get("ELEVEN_REF_DIR", "/root/reference/src/tfg-pathtracer")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+# --fmad=false: no multiply-add contraction in device code, so every kernel
+# that inlines the same shading code (the wavefront's shade, its gradient
+# variant, the replay walk) rounds every operation alike and their paths
+# agree bit for bit whatever register budget each kernel is compiled for;
+# explicit fmaf() (the slab tests) is unaffected.
+CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "--fmad=false", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 # extra nvcc flags (tuning sweeps); a change needs build_product(force=True)
 CU_FLAGS += os.environ.get("ELEVEN_NVCC_FLAGS", "").split()
