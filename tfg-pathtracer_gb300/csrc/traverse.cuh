@@ -80,7 +80,17 @@ __device__ __forceinline__ f3 ref_position(f3 o, f3 d, float t, float u, float v
   return convex ? sp : geom;
 }
 
-__device__ __forceinline__ float byte_of(uint32_t w, int c) { return (float)((w >> (8 * c)) & 0xFFu); }
+// Byte c of w as a float, exactly: the byte is placed in the low mantissa
+// bits of 2^23 (byte permute) and 2^23 subtracted, two full-rate
+// operations instead of a shift, a mask and an integer conversion.
+__device__ __forceinline__ float byte_of(uint32_t w, int c) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)c)) - 8388608.0f;
+}
+// Decoded Q8 plane origin + q * scale: q * scale is exact (q <= 255, the
+// scale a power of two), so the fused form rounds like the sum.
+__device__ __forceinline__ float q8_plane(float org, uint32_t w, int c, float scale) {
+  return fmaf(byte_of(w, c), scale, org);
+}
 
 // Three-input min / max (PTX ISA 8.8, sm_100+); a NaN input is ignored.
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -246,12 +256,12 @@ struct Traverser {
       uint32_t qnx = (sgn & 1u) ? b.y : b.x, qfx = (sgn & 1u) ? b.x : b.y;
       uint32_t qny = (sgn & 2u) ? b.w : b.z, qfy = (sgn & 2u) ? b.z : b.w;
       uint32_t qnz = (sgn & 4u) ? c.y : c.x, qfz = (sgn & 4u) ? c.x : c.y;
-      nx = make_float4(ox + byte_of(qnx, 0) * sx, ox + byte_of(qnx, 1) * sx, ox + byte_of(qnx, 2) * sx, ox + byte_of(qnx, 3) * sx);
-      fx = make_float4(ox + byte_of(qfx, 0) * sx, ox + byte_of(qfx, 1) * sx, ox + byte_of(qfx, 2) * sx, ox + byte_of(qfx, 3) * sx);
-      ny = make_float4(oy + byte_of(qny, 0) * sy, oy + byte_of(qny, 1) * sy, oy + byte_of(qny, 2) * sy, oy + byte_of(qny, 3) * sy);
-      fy = make_float4(oy + byte_of(qfy, 0) * sy, oy + byte_of(qfy, 1) * sy, oy + byte_of(qfy, 2) * sy, oy + byte_of(qfy, 3) * sy);
-      nz = make_float4(oz + byte_of(qnz, 0) * sz, oz + byte_of(qnz, 1) * sz, oz + byte_of(qnz, 2) * sz, oz + byte_of(qnz, 3) * sz);
-      fz = make_float4(oz + byte_of(qfz, 0) * sz, oz + byte_of(qfz, 1) * sz, oz + byte_of(qfz, 2) * sz, oz + byte_of(qfz, 3) * sz);
+      nx = make_float4(q8_plane(ox, qnx, 0, sx), q8_plane(ox, qnx, 1, sx), q8_plane(ox, qnx, 2, sx), q8_plane(ox, qnx, 3, sx));
+      fx = make_float4(q8_plane(ox, qfx, 0, sx), q8_plane(ox, qfx, 1, sx), q8_plane(ox, qfx, 2, sx), q8_plane(ox, qfx, 3, sx));
+      ny = make_float4(q8_plane(oy, qny, 0, sy), q8_plane(oy, qny, 1, sy), q8_plane(oy, qny, 2, sy), q8_plane(oy, qny, 3, sy));
+      fy = make_float4(q8_plane(oy, qfy, 0, sy), q8_plane(oy, qfy, 1, sy), q8_plane(oy, qfy, 2, sy), q8_plane(oy, qfy, 3, sy));
+      nz = make_float4(q8_plane(oz, qnz, 0, sz), q8_plane(oz, qnz, 1, sz), q8_plane(oz, qnz, 2, sz), q8_plane(oz, qnz, 3, sz));
+      fz = make_float4(q8_plane(oz, qfz, 0, sz), q8_plane(oz, qfz, 1, sz), q8_plane(oz, qfz, 2, sz), q8_plane(oz, qfz, 3, sz));
       ch = make_int4((int)c.z, (int)c.w, (int)e.x, (int)e.y);
       float dd = __uint_as_float(e.z);
       dl = make_float4(dd, dd, dd, dd);
