@@ -433,6 +433,7 @@ def run_adjoint(args):
     evaluations per second.  The check: central differences (h = 1e-3,
     common random numbers) of the detached estimator on --fd-params random
     parameters, at 16 spp."""
+    from eleven import _abi as A
     from eleven import _lib, scenes
     spp, depth = 64, 6
     arrays = scenes.config4()
@@ -445,7 +446,8 @@ def run_adjoint(args):
     n_params = m0.size + e0.size
 
     def step(seed):
-        out = s.render(spp, max_depth=depth, seed=seed)
+        # the forward keeps each sample's radiance for the backward pass
+        out = s.render(spp, max_depth=depth, seed=seed, flags=A.ER_RENDER_KEEP_PATHS)
         d = np.zeros_like(out["beauty"])
         d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
         gm, ge, st = s.backward(spp, d, out["samples"], max_depth=depth, seed=seed)

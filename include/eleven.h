@@ -191,6 +191,10 @@ enum {
   ER_RENDER_COUNT = 1u << 7,      /* count node visits / triangle tests     */
   ER_RENDER_SNAPSHOTS = 1u << 8,  /* copy the film to the snapshot buffer
                                      after every wave (er_snapshot)         */
+  ER_RENDER_KEEP_PATHS = 1u << 10, /* keep every sample's radiance on the
+                                     device, so that an er_backward with the
+                                     same options (and unchanged parameters
+                                     and camera) skips its forward pass     */
   ER_RENDER_ONE_STREAM = 1u << 9  /* run the waves one after another on the
                                      scene's stream.  Default with two or
                                      more waves: two waves in flight on two
@@ -346,7 +350,10 @@ er_status er_render_replay(er_scene* scene, const er_render_opts* opts, const fl
  * (W*H*4 floats, the film's layout), samples = that render's per-pixel
  * sample counts.  The derivative holds the sampling fixed (the detached
  * estimator er_render_replay evaluates).  Outputs: n_materials*5 and
- * env w*h*3 floats. */
+ * env w*h*3 floats.  The samples' radiance comes from the last er_render
+ * when it ran with ER_RENDER_KEEP_PATHS and the same seed, sample range,
+ * depth and env sampling, with no er_scene_set_params / set_camera since;
+ * otherwise er_backward renders them again first. */
 er_status er_backward(er_scene* scene, const er_render_opts* opts, const float* d_beauty, const uint32_t* samples,
                       float* grad_materials, float* grad_env, er_render_stats* stats);
 

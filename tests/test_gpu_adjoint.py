@@ -176,3 +176,47 @@ def test_gradients_match_fp64_oracle(small):
     assert max(errs) < 5e-2
     o64.close()
     orc.close()
+
+
+def test_kept_paths_give_the_same_gradient(small):
+    """er_render with ER_RENDER_KEEP_PATHS lets er_backward skip its forward
+    pass; the gradient is the one er_backward computes on its own (up to the
+    order of the float atomics), and a backward with other options, or after
+    a parameter change, does not use the kept radiance."""
+    arrays, s, T = small
+    m0, e0 = s.get_params()
+
+    def grads(seed, keep, other_seed=None):
+        out = s.render(SPP, max_depth=DEPTH, seed=seed, flags=A.ER_RENDER_KEEP_PATHS if keep else 0)
+        d = np.zeros_like(out["beauty"])
+        d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
+        bs = seed if other_seed is None else other_seed
+        gm, ge, _ = s.backward(SPP, d, out["samples"], max_depth=DEPTH, seed=bs)
+        return gm, ge, d, out["samples"]
+
+    def close(a, b):
+        np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-6 * max(np.abs(b).max(), 1e-30))
+
+    gm_k, ge_k, d, smp = grads(7, True)
+    gm_n, ge_n, _, _ = grads(7, False)
+    close(gm_k, gm_n)
+    close(ge_k, ge_n)
+    # kept radiance of seed 7, backward of seed 8: recomputed, not reused
+    s.render(SPP, max_depth=DEPTH, seed=7, flags=A.ER_RENDER_KEEP_PATHS)
+    gm_8a, ge_8a, _ = s.backward(SPP, d, smp, max_depth=DEPTH, seed=8)
+    s.render(SPP, max_depth=DEPTH, seed=1)
+    gm_8b, ge_8b, _ = s.backward(SPP, d, smp, max_depth=DEPTH, seed=8)
+    close(gm_8a, gm_8b)
+    close(ge_8a, ge_8b)
+    # a parameter change after the kept render: recomputed with the new parameters
+    s.render(SPP, max_depth=DEPTH, seed=7, flags=A.ER_RENDER_KEEP_PATHS)
+    m1 = m0.copy()
+    m1[:, 3] = np.clip(m1[:, 3] * 0.5, 0.05, 1.0)
+    s.set_params(m1, e0)
+    gm_c, ge_c, _ = s.backward(SPP, d, smp, max_depth=DEPTH, seed=7)
+    s.render(SPP, max_depth=DEPTH, seed=1)
+    gm_d, ge_d, _ = s.backward(SPP, d, smp, max_depth=DEPTH, seed=7)
+    close(gm_c, gm_d)
+    close(ge_c, ge_d)
+    assert not np.allclose(gm_c, gm_k)
+    s.set_params(m0, e0)

@@ -358,6 +358,7 @@ extern "C" er_status er_scene_get_params(er_scene* s, float* materials, float* e
 extern "C" er_status er_scene_set_params(er_scene* s, const float* materials, const float* env, uint32_t flags) {
   if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
   ER_CUDA(cudaSetDevice(s->device));
+  s->version++;  // radiance kept by an earlier render no longer applies
   const bool dev = flags & ER_RENDER_DEVICE_OUT;
   const int32_t nm = s->dev.n_mats;
   if (materials && nm > 0) {
@@ -475,17 +476,34 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
   else if ((st = T.alloc((void**)&A.g_env, env_n * 4)) != ER_OK) return st;
   ER_CUDA(cudaMemsetAsync(A.g_mat, 0, mat_n * 4, s->stream));
   ER_CUDA(cudaMemsetAsync(A.g_env, 0, env_n * 4, s->stream));
-  // the samples' radiance: the wavefront forward, one wave, per-path dump
+  // the samples' radiance: the wavefront forward with a per-path dump into
+  // scratch kept on the scene (grown, never shrunk, between calls)
   const int64_t npaths = (int64_t)np * A.P.spp_wave;
-  float* d_rad = nullptr;
-  int32_t* d_b = nullptr;
-  if ((st = T.alloc((void**)&d_rad, (size_t)npaths * 12)) != ER_OK) return st;
-  if ((st = T.alloc((void**)&d_b, (size_t)npaths * 4)) != ER_OK) return st;
+  const bool kept = s->kp_valid && s->kp_version == s->version && s->kp_seed == o->seed &&
+                    s->kp_begin == o->sample_begin && s->kp_spp == o->spp &&
+                    s->kp_depth == (o->max_depth > 0 ? o->max_depth : 5) &&
+                    s->kp_flags == (o->flags & ER_RENDER_ENV_ALIAS);
+  if (!kept && npaths > s->bw_cap) {
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(s->bw_rad);
+    cudaFree(s->bw_b);
+    s->bw_rad = nullptr;
+    s->bw_b = nullptr;
+    s->bw_cap = 0;
+    if (cudaMalloc(&s->bw_rad, (size_t)npaths * 12) != cudaSuccess ||
+        cudaMalloc(&s->bw_b, (size_t)npaths * 4) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ER_ERR_OOM, "adjoint scratch allocation failed");
+    }
+    s->bw_cap = npaths;
+  }
+  float* d_rad = kept ? s->kp_rad : s->bw_rad;
+  int32_t* d_b = s->bw_b;
   ER_CUDA(cudaEventRecord(s->ev0, s->stream));
   if (npaths > 0) {
     er_render_opts oo = *o;
     oo.flags &= ER_RENDER_ENV_ALIAS;
-    if ((st = render_paths_device(s, &oo, d_rad, d_b)) != ER_OK) return st;
+    if (!kept && (st = render_paths_device(s, &oo, d_rad, d_b, true)) != ER_OK) return st;
     GradArgs G;
     G.rad = d_rad;
     G.d_beauty = A.d_beauty;

@@ -144,6 +144,68 @@ static __device__ D3 disney_eval_d(const HitData& hd, D3 Cdlin, Dual rough, Dual
   return diff + spec + d3c(cc);
 }
 
+// Closed-form partials of DisneyEval (Disney.hpp:179-253) in albedo and
+// metallic.  With GD = Gs * Ds, A the specular mix and Ctint = Cdlin /
+// Cdlum (Cdlum = 0.3 r + 0.6 g + 0.1 b):
+//   f_c = (Cdlin_c kd + Fsheen_c)(1 - m) + (Cspec0_c (1 - FH) + FH) GD + cc
+//   Cspec0_c = X_c (1 - m) + m Cdlin_c,  X_c = (1 + sT (Ctint_c - 1)) 0.08 s
+//   Fsheen_c = (1 + shT (Ctint_c - 1)) FH sheen
+// so  d f_c / d Cdlin_j = [c = j] (kd (1 - m) + GD (1 - FH) m)
+//                         + d Ctint_c / d Cdlin_j (1 - m)(shT FH sheen + GD (1 - FH) sT 0.08 s)
+// with d Ctint_c / d Cdlin_j = ([c = j] - Ctint_c w_j) / Cdlum (zero when
+// Cdlum <= 0, where Ctint is the constant 1), and
+//   d f_c / d m = -(Cdlin_c kd + Fsheen_c) + GD (1 - FH)(Cdlin_c - X_c).
+// dA[j] holds d f / d Cdlin_j for the three channels.
+struct EvalGrad {
+  f3 dA[3];
+  f3 dM;
+};
+__device__ __forceinline__ EvalGrad disney_eval_grad(const HitData& hd, const DisneyCtx& c, f3 L) {
+  EvalGrad g;
+  g.dA[0] = g.dA[1] = g.dA[2] = g.dM = mk1(0.f);
+  if (!(hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f)) return g;
+  const f3 H = normalized(L + c.V);
+  const float NDotL = fabsf(dot(c.N, L));
+  const float NDotV = fabsf(dot(c.N, c.V));
+  const float NDotH = fabsf(dot(c.N, H));
+  const float LDotH = fabsf(dot(L, H));
+  const f3 Cdlin = hd.albedo;
+  const float m = hd.metallic;
+  const float Cdlum = 0.3f * Cdlin.x + 0.6f * Cdlin.y + 0.1f * Cdlin.z;
+  const bool lum = Cdlum > 0.0f;
+  const f3 Ctint = lum ? Cdlin / Cdlum : mk1(1.0f);
+  const float s08 = hd.specular * 0.08f;
+  const f3 X = lerp3(mk1(1.0f), Ctint, hd.specularTint) * s08;
+  const f3 Csheen = lerp3(mk1(1.0f), Ctint, hd.sheenTint);
+  const float FL = schlick(NDotL), FV = schlick(NDotV);
+  const float Fd90 = 0.5f + 2.0f * LDotH * LDotH * hd.roughness;
+  const float Fd = lerpf_(1.0f, Fd90, FL) * lerpf_(1.0f, Fd90, FV);
+  const float Fss90 = LDotH * LDotH * hd.roughness;
+  const float Fss = lerpf_(1.0f, Fss90, FL) * lerpf_(1.0f, Fss90, FV);
+  const float ss = 1.25f * (Fss * (1.0f / (NDotL + NDotV) - 0.5f) + 0.5f);
+  const float Ds = gtr2_aniso(NDotH, dot(H, c.T), dot(H, c.B), c.ax, c.ay);
+  const float FH = schlick(LDotH);
+  const float Gs = smith_ggx_aniso(NDotL, dot(L, c.T), dot(L, c.B), c.ax, c.ay) *
+                   smith_ggx_aniso(NDotV, dot(c.V, c.T), dot(c.V, c.B), c.ax, c.ay);
+  const float GD = Gs * Ds;
+  const float kd = (1.0f / ER_PI) * lerpf_(Fd, ss, hd.subsurface);
+  const f3 Fsheen = Csheen * (FH * hd.sheen);
+  const float spec_m = GD * (1.0f - FH);
+  g.dM = (Cdlin - X) * spec_m - (Cdlin * kd + Fsheen);
+  const float A = kd * (1.0f - m) + spec_m * m;
+  const float B = lum ? (1.0f - m) * (hd.sheenTint * FH * hd.sheen + spec_m * hd.specularTint * s08) / Cdlum : 0.0f;
+  const float w[3] = {0.3f, 0.6f, 0.1f};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    g.dA[j] = Ctint * (-B * w[j]);
+    const float diag = A + B;
+    if (j == 0) g.dA[j].x += diag;
+    if (j == 1) g.dA[j].y += diag;
+    if (j == 2) g.dA[j].z += diag;
+  }
+  return g;
+}
+
 // base[key * N + k] += v[k], warp-aggregated: the converged lanes that
 // share a key (neighbouring pixels see the same env texel and object) are
 // summed with shuffles and one lane issues the N atomics.  Non-finite
@@ -182,7 +244,6 @@ __device__ __forceinline__ void vertex_gradient(const DevScene& S, const VertexS
                                                 float* g_env) {
   const DevMaterial& M = S.mats[V.mat];
   const f3 f = V.f, fH = V.fH, eH = V.eH;
-  // one parameter at a time (single-partial duals keep registers low)
   const bool ca = M.albedo_tex < 0, cr = M.roughness_tex < 0, cm = M.metallic_tex < 0;
   const DisneyCtx& C = V.C;
   // strategy weights per channel: C_c = thr_c * (kH_c fH_c + kP_c fP_c + kB_c f_c)
@@ -194,29 +255,38 @@ __device__ __forceinline__ void vertex_gradient(const DevScene& S, const VertexS
   const f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
   const f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
                    f.z != 0.f ? dl.z * La.z / f.z : 0.f);
-  float gk[kParams];
-#pragma unroll 1
-  for (int k = 0; k < kParams; k++) {
+  // albedo and metallic: closed-form partials of the three evaluations
+  float gk[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const bool use_p = V.has_pt && vP;
+  const bool dm = cm && V.metal_in > 0.f;
+  if (ca || dm) {
+    const f3 uB = mk(wd.x * kB.x + ra.x, wd.y * kB.y + ra.y, wd.z * kB.z + ra.z);
+    const f3 uH = mk(wd.x * kH.x, wd.y * kH.y, wd.z * kH.z);
+    const f3 uP = mk(wd.x * kP.x, wd.y * kP.y, wd.z * kP.z);
+    const EvalGrad G = disney_eval_grad(V.hd, C, V.dir);
+    const EvalGrad GH = disney_eval_grad(V.hd, C, V.dH);
+    EvalGrad GP;
+    GP.dA[0] = GP.dA[1] = GP.dA[2] = GP.dM = mk1(0.f);
+    if (use_p) GP = disney_eval_grad(V.hd, C, V.dP);
+    if (ca)
+#pragma unroll
+      for (int j = 0; j < 3; j++) gk[j] = dot(uB, G.dA[j]) + dot(uH, GH.dA[j]) + dot(uP, GP.dA[j]);
+    if (dm) gk[4] = 2.2f * powf(V.metal_in, 1.2f) * (dot(uB, G.dM) + dot(uH, GH.dM) + dot(uP, GP.dM));
+  }
+  // roughness: a single-partial dual through the three evaluations
+  if (cr && V.rough_in > 0.f) {
     D3 alb{dconst(V.hd.albedo.x), dconst(V.hd.albedo.y), dconst(V.hd.albedo.z)};
     Dual rg = dconst(V.hd.roughness), mt = dconst(V.hd.metallic);
-    bool seeded = false;
-    if (k == 0 && ca) { alb.x.d[0] = 1.f; seeded = true; }
-    if (k == 1 && ca) { alb.y.d[0] = 1.f; seeded = true; }
-    if (k == 2 && ca) { alb.z.d[0] = 1.f; seeded = true; }
-    if (k == 3 && cr && V.rough_in > 0.f) { rg.d[0] = 2.2f * powf(V.rough_in, 1.2f); seeded = true; }
-    if (k == 4 && cm && V.metal_in > 0.f) { mt.d[0] = 2.2f * powf(V.metal_in, 1.2f); seeded = true; }
-    float acc = 0.f;
-    if (seeded) {
-      D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
-      D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
-      acc = wd.x * (kH.x * DfH.x.d[0] + kB.x * Df.x.d[0]) + wd.y * (kH.y * DfH.y.d[0] + kB.y * Df.y.d[0]) +
-            wd.z * (kH.z * DfH.z.d[0] + kB.z * Df.z.d[0]) + ra.x * Df.x.d[0] + ra.y * Df.y.d[0] + ra.z * Df.z.d[0];
-      if (V.has_pt && vP) {
-        D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
-        acc += wd.x * kP.x * DfP.x.d[0] + wd.y * kP.y * DfP.y.d[0] + wd.z * kP.z * DfP.z.d[0];
-      }
+    rg.d[0] = 2.2f * powf(V.rough_in, 1.2f);
+    D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
+    D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
+    float acc = wd.x * (kH.x * DfH.x.d[0] + kB.x * Df.x.d[0]) + wd.y * (kH.y * DfH.y.d[0] + kB.y * Df.y.d[0]) +
+                wd.z * (kH.z * DfH.z.d[0] + kB.z * Df.z.d[0]) + ra.x * Df.x.d[0] + ra.y * Df.y.d[0] + ra.z * Df.z.d[0];
+    if (use_p) {
+      D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
+      acc += wd.x * kP.x * DfP.x.d[0] + wd.y * kP.y * DfP.y.d[0] + wd.z * kP.z * DfP.z.d[0];
     }
-    gk[k] = acc;
+    gk[3] = acc;
   }
   agg_add<kParams>(g_mat, V.mat, gk);
   if (vH) {

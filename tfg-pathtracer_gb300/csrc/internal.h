@@ -154,6 +154,11 @@ struct Film {
   uint32_t* samples = nullptr;
   uint32_t* pathcount = nullptr;
   bool aov_on = false;
+  // optional per-sample radiance (before the clamp), 3 floats at
+  // (sample - first sample) * npix + pixel index; keep_s0 = the wave's
+  // first sample relative to the call's
+  float* keep = nullptr;
+  int32_t keep_s0 = 0;
 };
 
 struct Wave;  // wavefront buffers (render.cu)
@@ -233,6 +238,20 @@ struct er_scene {
   int num_sms = 0;
   er::Film film;
   er::Wave* wave = nullptr;
+  // adjoint scratch kept between er_backward calls: per-path radiance and
+  // vertex counts of the dumped forward pass, gradient accumulators
+  float* bw_rad = nullptr;
+  int32_t* bw_b = nullptr;
+  int64_t bw_cap = 0;
+  // radiance kept by er_render (ER_RENDER_KEEP_PATHS) and the options it
+  // belongs to; `version` counts parameter and camera changes
+  float* kp_rad = nullptr;
+  int64_t kp_cap = 0;
+  bool kp_valid = false;
+  uint64_t kp_seed = 0;
+  int32_t kp_begin = 0, kp_spp = 0, kp_depth = 0;
+  uint32_t kp_flags = 0;
+  uint64_t kp_version = 0, version = 0;
   // second wave in flight (its own buffers and stream), so that one wave's
   // launches fill the other's traversal tails
   er::Wave* wave2 = nullptr;
@@ -286,8 +305,10 @@ struct GradArgs {
 er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G);
 // Per-path radiance (spp x npix x 3, sample-major, output index order) and
 // vertex counts of the samples er_render makes with opts, into device
-// buffers, in one wave (render.cu).
-er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b);
+// buffers (render.cu).  grad_wave: size the wave buffers for the gradient
+// wavefront that follows, so that it reuses them.
+er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b,
+                              bool grad_wave = false);
 // Wavefront buffers for `cap` paths (render.cu); stats = device ray counters.
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out);
 void wave_destroy(Wave* w);

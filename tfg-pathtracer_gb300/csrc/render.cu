@@ -485,6 +485,10 @@ __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WavePa
     int32_t p = path_base + s * P.npix + pix;
     float4 L = w.light[p];
     resolve(w, p, L);
+    if (F.keep) {
+      float* r = F.keep + 3 * ((int64_t)(F.keep_s0 + s) * P.npix + idx);
+      r[0] = L.x; r[1] = L.y; r[2] = L.z;
+    }
     pc += (uint32_t)w.bounces[p];
     bounce_sum += (uint32_t)w.bounces[p];
     float lx = clampf_(L.x, 0.f, 10.f), ly = clampf_(L.y, 0.f, 10.f), lz = clampf_(L.z, 0.f, 10.f);
@@ -526,13 +530,14 @@ __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WavePa
 }
 
 // Per-path dump for er_render_paths.
-__global__ void k_dump(WaveView w, WaveParams P, int32_t sw, float* rad, int32_t* bnc) {
+// s_off: the wave's first sample, relative to the call's first.
+__global__ void k_dump(WaveView w, WaveParams P, int32_t sw, int32_t s_off, float* rad, int32_t* bnc) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= sw * P.npix) return;
   float4 L = w.light[p];
   resolve(w, p, L);
   int32_t pix = p % P.npix, s = p / P.npix;
-  int64_t j = (int64_t)s * P.npix + out_index(P, pix % P.W, pix / P.W);
+  int64_t j = (int64_t)(s + s_off) * P.npix + out_index(P, pix % P.W, pix / P.W);
   rad[3 * j] = L.x; rad[3 * j + 1] = L.y; rad[3 * j + 2] = L.z;
   bnc[j] = w.bounces[p];
 }
@@ -679,15 +684,15 @@ er_status copy_out(er_scene* s, bool dev, void* dst, const void* src, size_t byt
 }
 
 // Runs the waves of one call.  dump_rad != null: single wave, per-path dump.
-er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* dump_b, int64_t* launches) {
+er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* dump_b, int64_t* launches,
+              bool grad_wave = false) {
   const int32_t W = s->camera.x_res, H = s->camera.y_res;
   const int32_t npix = W * H;
   const bool aov = o->flags & ER_RENDER_AOV;
   int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
   int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : std::max(1, (int32_t)((int64_t)(1 << 22) / npix));
   sw = std::min(sw, std::max(1, o->spp));
-  if (dump_rad) sw = o->spp;
-  er_status st = ensure_wave(s, (int64_t)sw * npix, aov);
+  er_status st = ensure_wave(s, (int64_t)sw * npix, aov, grad_wave);
   if (st != ER_OK) return st;
   WaveParams P;
   P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
@@ -766,9 +771,13 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
     }
     if (dump_rad) {
-      k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, dump_rad, dump_b);
+      k_dump<<<(n + 255) / 256, 256, 0, s->stream>>>(w, P, cur, s0, dump_rad, dump_b);
     } else {
       Film F = s->film;
+      if (o->flags & ER_RENDER_KEEP_PATHS) {
+        F.keep = s->kp_rad;
+        F.keep_s0 = s0;
+      }
       if (two && k > 0) ER_CUDA(cudaStreamWaitEvent(strm, s->ev_acc[(k - 1) & 1], 0));
       k_accumulate<false><<<(npix + 127) / 128, 128, 0, strm>>>(w, P, F, cur, NB);
       if (o->flags & ER_RENDER_SNAPSHOTS) {
@@ -844,10 +853,10 @@ void free_film(er_scene* s) {
   F = Film();
 }
 
-er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b) {
+er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b, bool grad_wave) {
   er_render_opts oo = *o;
   oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
-  return run(s, &oo, d_rad, d_b, nullptr);
+  return run(s, &oo, d_rad, d_b, nullptr, grad_wave);
 }
 
 // The gradient wavefront: the same waves as run(), with the gradient
@@ -1043,11 +1052,36 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
   if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
   if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
   if ((o->flags & ER_RENDER_SNAPSHOTS) && (st = ensure_snapshot(s)) != ER_OK) return st;
+  const bool keep = o->flags & ER_RENDER_KEEP_PATHS;
+  s->kp_valid = false;
+  if (keep) {
+    const int64_t need = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
+    if (need > s->kp_cap) {
+      ER_CUDA(cudaStreamSynchronize(s->stream));
+      cudaFree(s->kp_rad);
+      s->kp_rad = nullptr;
+      s->kp_cap = 0;
+      if (cudaMalloc(&s->kp_rad, (size_t)std::max<int64_t>(need, 1) * 12) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ER_ERR_OOM, "kept-path radiance allocation failed");
+      }
+      s->kp_cap = need;
+    }
+  }
   unsigned long long st0[8];
   ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
   ER_CUDA(cudaEventRecord(s->ev0, s->stream));
   int64_t launches = 0;
   if ((st = run(s, o, nullptr, nullptr, &launches)) != ER_OK) return st;
+  if (keep) {
+    s->kp_valid = true;
+    s->kp_seed = o->seed;
+    s->kp_begin = o->sample_begin;
+    s->kp_spp = o->spp;
+    s->kp_depth = o->max_depth > 0 ? o->max_depth : 5;
+    s->kp_flags = o->flags & ER_RENDER_ENV_ALIAS;
+    s->kp_version = s->version;
+  }
   ER_CUDA(cudaEventRecord(s->ev1, s->stream));
   if (!(o->flags & ER_RENDER_NO_OUTPUT)) {
     uint32_t fl = o->flags & ER_RENDER_DEVICE_OUT;

@@ -405,6 +405,7 @@ extern "C" er_status er_scene_set_camera(er_scene* s, const er_camera* c) {
     return fail(ER_ERR_INVALID_ARG, "camera resolution out of range");
   s->camera = *c;
   s->dev.cam = make_dev_camera(*c);
+  s->version++;
   return ER_OK;
 }
 
@@ -420,6 +421,9 @@ extern "C" er_status er_scene_free(er_scene* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_wave(s);
   free_film(s);
+  cudaFree(s->bw_rad);
+  cudaFree(s->bw_b);
+  cudaFree(s->kp_rad);
   for (void* p : s->allocs) cudaFree(p);
   s->allocs.clear();
   for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);

@@ -131,6 +131,7 @@ ER_RENDER_PROFILE = 1 << 6
 ER_RENDER_COUNT = 1 << 7
 ER_RENDER_SNAPSHOTS = 1 << 8
 ER_RENDER_ONE_STREAM = 1 << 9
+ER_RENDER_KEEP_PATHS = 1 << 10
 STAGES = ["raygen", "trace", "shade", "reserved", "accumulate"]
 
 

@@ -40,12 +40,14 @@ class RenderFunction(torch.autograd.Function):
             beauty = torch.empty((H * W, 4), dtype=torch.float32, device=m.device)
             samples = torch.empty((H * W,), dtype=torch.int32, device=m.device)
             pc = torch.empty((H * W,), dtype=torch.int32, device=m.device)
-            o.flags = A.ER_RENDER_DEVICE_OUT
+            # keep the samples' radiance for the backward pass
+            o.flags = A.ER_RENDER_DEVICE_OUT | A.ER_RENDER_KEEP_PATHS
             _lib.check(L.er_render(scene.h, C.byref(o), _ptr(beauty), None, None, None, _ptr(samples), _ptr(pc), None),
                        "er_render")
         else:
             scene.set_params(materials.detach().float().numpy(), env.detach().float().numpy())
-            out = scene.render(spp, max_depth=max_depth, seed=seed, sample_begin=sample_begin)
+            out = scene.render(spp, max_depth=max_depth, seed=seed, sample_begin=sample_begin,
+                               flags=A.ER_RENDER_KEEP_PATHS)
             beauty = torch.from_numpy(out["beauty"])
             samples = torch.from_numpy(out["samples"].view(np.int32))
         ctx.scene = scene
