@@ -7,145 +7,10 @@
 
 namespace er {
 
-// ---------------------------------------------------------------- duals --
-// Forward-mode dual number carrying the derivative along one material
-// parameter (the replay loops over the kParams parameters of a vertex).
-constexpr int kNP = 1;
-constexpr int kParams = 5;  // albedo r, g, b, roughness, metallic
+constexpr int kParams = 5;  // per material: albedo r, g, b, roughness, metallic
 
-struct Dual {
-  float v;
-  float d[kNP];
-};
-
-__device__ __forceinline__ Dual dconst(float v) {
-  Dual r;
-  r.v = v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = 0.f;
-  return r;
-}
-__device__ __forceinline__ Dual operator+(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v + b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] + b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator-(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v - b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] - b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v * b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-  Dual r;
-  r.v = a.v / b.v;
-  float ib = 1.0f / b.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
-  return r;
-}
-__device__ __forceinline__ Dual operator+(Dual a, float b) { a.v += b; return a; }
-__device__ __forceinline__ Dual operator+(float b, Dual a) { a.v += b; return a; }
-__device__ __forceinline__ Dual operator-(float b, Dual a) {
-  Dual r;
-  r.v = b - a.v;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = -a.d[k];
-  return r;
-}
-__device__ __forceinline__ Dual operator*(Dual a, float b) {
-  a.v *= b;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) a.d[k] *= b;
-  return a;
-}
-__device__ __forceinline__ Dual operator*(float b, Dual a) { return a * b; }
-__device__ __forceinline__ Dual operator/(Dual a, float b) { return a * (1.0f / b); }
-__device__ __forceinline__ Dual operator/(float a, Dual b) { return dconst(a) / b; }
-__device__ __forceinline__ Dual dsqrt(Dual a) {
-  Dual r;
-  r.v = sqrtf(a.v);
-  float k2 = r.v > 0.f ? 0.5f / r.v : 0.f;
-#pragma unroll
-  for (int k = 0; k < kNP; k++) r.d[k] = a.d[k] * k2;
-  return r;
-}
-// maxf_(lo, a) of the reference: lo > a ? lo : a
-__device__ __forceinline__ Dual dmax_lo(float lo, Dual a) { return lo > a.v ? dconst(lo) : a; }
-__device__ __forceinline__ Dual dlerp(Dual a, Dual b, Dual c) { return a + c * (b - a); }
-
-struct D3 {
-  Dual x, y, z;
-};
-__device__ __forceinline__ D3 d3(Dual a) { return D3{a, a, a}; }
-__device__ __forceinline__ D3 d3c(float a) { return d3(dconst(a)); }
-__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ D3 operator*(D3 a, Dual s) { return D3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ D3 operator*(D3 a, float s) { return D3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ D3 dlerp3(D3 a, D3 b, Dual c) { return D3{dlerp(a.x, b.x, c), dlerp(a.y, b.y, c), dlerp(a.z, b.z, c)}; }
-__device__ __forceinline__ D3 dlerp3(D3 a, D3 b, float c) {
-  return D3{dlerp(a.x, b.x, dconst(c)), dlerp(a.y, b.y, dconst(c)), dlerp(a.z, b.z, dconst(c))};
-}
-
-__device__ __forceinline__ Dual gtr2_aniso_d(float NDotH, float HDotX, float HDotY, Dual ax, Dual ay) {
-  Dual a = HDotX / ax, b = HDotY / ay;
-  Dual c = a * a + b * b + NDotH * NDotH;
-  return 1.0f / (ER_PI * ax * ay * c * c);
-}
-__device__ __forceinline__ Dual smith_ggx_aniso_d(float NDotV, float VDotX, float VDotY, Dual ax, Dual ay) {
-  Dual a = VDotX * ax, b = VDotY * ay;
-  return 1.0f / (NDotV + dsqrt(a * a + b * b + NDotV * NDotV));
-}
-
-// DisneyEval (Disney.hpp:179-253) with albedo, roughness and metallic as
-// duals; the other parameters and all directions are constants.
-static __device__ D3 disney_eval_d(const HitData& hd, D3 Cdlin, Dual rough, Dual metal, const DisneyCtx& c, f3 L) {
-  if (!(hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f)) return d3c(0.f);
-  f3 H = normalized(L + c.V);
-  float NDotL = fabsf(dot(c.N, L));
-  float NDotV = fabsf(dot(c.N, c.V));
-  float NDotH = fabsf(dot(c.N, H));
-  float LDotH = fabsf(dot(L, H));
-  Dual Cdlum = Cdlin.x * 0.3f + Cdlin.y * 0.6f + Cdlin.z * 0.1f;
-  D3 Ctint = Cdlum.v > 0.0f ? D3{Cdlin.x / Cdlum, Cdlin.y / Cdlum, Cdlin.z / Cdlum} : d3c(1.0f);
-  D3 Cspec0 = dlerp3(dlerp3(d3c(1.0f), Ctint, hd.specularTint) * (hd.specular * 0.08f), Cdlin, metal);
-  D3 Csheen = dlerp3(d3c(1.0f), Ctint, hd.sheenTint);
-  float FL = schlick(NDotL), FV = schlick(NDotV);
-  Dual Fd90 = 0.5f + rough * (2.0f * LDotH * LDotH);
-  Dual Fd = dlerp(dconst(1.0f), Fd90, dconst(FL)) * dlerp(dconst(1.0f), Fd90, dconst(FV));
-  Dual Fss90 = rough * (LDotH * LDotH);
-  Dual Fss = dlerp(dconst(1.0f), Fss90, dconst(FL)) * dlerp(dconst(1.0f), Fss90, dconst(FV));
-  Dual ss = (Fss * (1.0f / (NDotL + NDotV) - 0.5f) + 0.5f) * 1.25f;
-  float aspect = sqrtf(1.0f - hd.anisotropic * 0.9f);
-  Dual ax = dmax_lo(0.001f, rough / aspect), ay = dmax_lo(0.001f, rough * aspect);
-  Dual Ds = gtr2_aniso_d(NDotH, dot(H, c.T), dot(H, c.B), ax, ay);
-  float FH = schlick(LDotH);
-  D3 Fs = dlerp3(Cspec0, d3c(1.0f), FH);
-  Dual Gs = smith_ggx_aniso_d(NDotL, dot(L, c.T), dot(L, c.B), ax, ay) *
-            smith_ggx_aniso_d(NDotV, dot(c.V, c.T), dot(c.V, c.B), ax, ay);
-  D3 Fsheen = Csheen * (FH * hd.sheen);
-  float Dr = gtr1(NDotH, c.clearcoatAlpha);
-  float Fr = lerpf_(0.04f, 1.0f, FH);
-  float Gr = smith_ggx(NDotL, 0.25f) * smith_ggx(NDotV, 0.25f);
-  Dual kd = dlerp(Fd, ss, dconst(hd.subsurface)) * (1.0f / ER_PI);
-  D3 diff = (Cdlin * kd + Fsheen) * (1.0f - metal);
-  D3 spec = Fs * (Gs * Ds);
-  float cc = 0.25f * hd.clearcoat * Gr * Fr * Dr;
-  return diff + spec + d3c(cc);
-}
-
-// Closed-form partials of DisneyEval (Disney.hpp:179-253) in albedo and
-// metallic.  With GD = Gs * Ds, A the specular mix and Ctint = Cdlin /
+// Closed-form partials of DisneyEval (Disney.hpp:179-253) in albedo,
+// metallic and roughness.  With GD = Gs * Ds, A the specular mix and Ctint = Cdlin /
 // Cdlum (Cdlum = 0.3 r + 0.6 g + 0.1 b):
 //   f_c = (Cdlin_c kd + Fsheen_c)(1 - m) + (Cspec0_c (1 - FH) + FH) GD + cc
 //   Cspec0_c = X_c (1 - m) + m Cdlin_c,  X_c = (1 + sT (Ctint_c - 1)) 0.08 s
@@ -155,14 +20,22 @@ static __device__ D3 disney_eval_d(const HitData& hd, D3 Cdlin, Dual rough, Dual
 // with d Ctint_c / d Cdlin_j = ([c = j] - Ctint_c w_j) / Cdlum (zero when
 // Cdlum <= 0, where Ctint is the constant 1), and
 //   d f_c / d m = -(Cdlin_c kd + Fsheen_c) + GD (1 - FH)(Cdlin_c - X_c).
+// Roughness r enters kd through Fd90 = 0.5 + 2 LH^2 r and Fss90 = LH^2 r,
+// and GD through ax = max(0.001, r / aspect), ay = max(0.001, r aspect):
+//   d f_c / d r = Cdlin_c (1 - m) d kd / d r + Fs_c d GD / d r
+//   Ds = 1 / (pi ax ay q^2), q = (HX / ax)^2 + (HY / ay)^2 + NH^2:
+//     d Ds / d ax = Ds (4 HX^2 / (ax^3 q) - 1 / ax)   (ay alike)
+//   G1 = 1 / (NV + S), S = sqrt((VX ax)^2 + (VY ay)^2 + NV^2):
+//     d G1 / d ax = -G1^2 VX^2 ax / S                  (ay alike)
 // dA[j] holds d f / d Cdlin_j for the three channels.
 struct EvalGrad {
   f3 dA[3];
   f3 dM;
+  f3 dR;
 };
 __device__ __forceinline__ EvalGrad disney_eval_grad(const HitData& hd, const DisneyCtx& c, f3 L) {
   EvalGrad g;
-  g.dA[0] = g.dA[1] = g.dA[2] = g.dM = mk1(0.f);
+  g.dA[0] = g.dA[1] = g.dA[2] = g.dM = g.dR = mk1(0.f);
   if (!(hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f)) return g;
   const f3 H = normalized(L + c.V);
   const float NDotL = fabsf(dot(c.N, L));
@@ -183,12 +56,39 @@ __device__ __forceinline__ EvalGrad disney_eval_grad(const HitData& hd, const Di
   const float Fss90 = LDotH * LDotH * hd.roughness;
   const float Fss = lerpf_(1.0f, Fss90, FL) * lerpf_(1.0f, Fss90, FV);
   const float ss = 1.25f * (Fss * (1.0f / (NDotL + NDotV) - 0.5f) + 0.5f);
-  const float Ds = gtr2_aniso(NDotH, dot(H, c.T), dot(H, c.B), c.ax, c.ay);
+  const float HX = dot(H, c.T), HY = dot(H, c.B);
+  const float Ds = gtr2_aniso(NDotH, HX, HY, c.ax, c.ay);
   const float FH = schlick(LDotH);
-  const float Gs = smith_ggx_aniso(NDotL, dot(L, c.T), dot(L, c.B), c.ax, c.ay) *
-                   smith_ggx_aniso(NDotV, dot(c.V, c.T), dot(c.V, c.B), c.ax, c.ay);
+  const float LX = dot(L, c.T), LY = dot(L, c.B), VX = dot(c.V, c.T), VY = dot(c.V, c.B);
+  const float G1L = smith_ggx_aniso(NDotL, LX, LY, c.ax, c.ay);
+  const float G1V = smith_ggx_aniso(NDotV, VX, VY, c.ax, c.ay);
+  const float Gs = G1L * G1V;
   const float GD = Gs * Ds;
   const float kd = (1.0f / ER_PI) * lerpf_(Fd, ss, hd.subsurface);
+  {
+    // roughness
+    const float LH2 = LDotH * LDotH;
+    const float dFd = 2.0f * LH2 * (FL * lerpf_(1.0f, Fd90, FV) + FV * lerpf_(1.0f, Fd90, FL));
+    const float dFss = LH2 * (FL * lerpf_(1.0f, Fss90, FV) + FV * lerpf_(1.0f, Fss90, FL));
+    const float dss = 1.25f * (1.0f / (NDotL + NDotV) - 0.5f) * dFss;
+    const float dkd = (1.0f / ER_PI) * ((1.0f - hd.subsurface) * dFd + hd.subsurface * dss);
+    const float aspect = sqrtf(1.0f - hd.anisotropic * 0.9f);
+    const float dax = hd.roughness / aspect > 0.001f ? 1.0f / aspect : 0.0f;
+    const float day = hd.roughness * aspect > 0.001f ? aspect : 0.0f;
+    const float q = (HX / c.ax) * (HX / c.ax) + (HY / c.ay) * (HY / c.ay) + NDotH * NDotH;
+    const float dDs_ax = Ds * (4.0f * HX * HX / (c.ax * c.ax * c.ax * q) - 1.0f / c.ax);
+    const float dDs_ay = Ds * (4.0f * HY * HY / (c.ay * c.ay * c.ay * q) - 1.0f / c.ay);
+    const float SL = sqrtf(LX * c.ax * (LX * c.ax) + LY * c.ay * (LY * c.ay) + NDotL * NDotL);
+    const float SV = sqrtf(VX * c.ax * (VX * c.ax) + VY * c.ay * (VY * c.ay) + NDotV * NDotV);
+    const float dG1L_ax = -G1L * G1L * LX * LX * c.ax / SL, dG1L_ay = -G1L * G1L * LY * LY * c.ay / SL;
+    const float dG1V_ax = -G1V * G1V * VX * VX * c.ax / SV, dG1V_ay = -G1V * G1V * VY * VY * c.ay / SV;
+    const float dGD_ax = (dG1L_ax * G1V + G1L * dG1V_ax) * Ds + Gs * dDs_ax;
+    const float dGD_ay = (dG1L_ay * G1V + G1L * dG1V_ay) * Ds + Gs * dDs_ay;
+    const float dGD = dGD_ax * dax + dGD_ay * day;
+    const f3 Cspec0 = lerp3(X, Cdlin, m);
+    const f3 Fs = lerp3(Cspec0, mk1(1.0f), FH);
+    g.dR = Cdlin * ((1.0f - m) * dkd) + Fs * dGD;
+  }
   const f3 Fsheen = Csheen * (FH * hd.sheen);
   const float spec_m = GD * (1.0f - FH);
   g.dM = (Cdlin - X) * spec_m - (Cdlin * kd + Fsheen);
@@ -255,38 +155,25 @@ __device__ __forceinline__ void vertex_gradient(const DevScene& S, const VertexS
   const f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
   const f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
                    f.z != 0.f ? dl.z * La.z / f.z : 0.f);
-  // albedo and metallic: closed-form partials of the three evaluations
+  // closed-form partials of the three evaluations
   float gk[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const bool use_p = V.has_pt && vP;
   const bool dm = cm && V.metal_in > 0.f;
-  if (ca || dm) {
+  const bool dr = cr && V.rough_in > 0.f;
+  if (ca || dm || dr) {
     const f3 uB = mk(wd.x * kB.x + ra.x, wd.y * kB.y + ra.y, wd.z * kB.z + ra.z);
     const f3 uH = mk(wd.x * kH.x, wd.y * kH.y, wd.z * kH.z);
     const f3 uP = mk(wd.x * kP.x, wd.y * kP.y, wd.z * kP.z);
     const EvalGrad G = disney_eval_grad(V.hd, C, V.dir);
     const EvalGrad GH = disney_eval_grad(V.hd, C, V.dH);
     EvalGrad GP;
-    GP.dA[0] = GP.dA[1] = GP.dA[2] = GP.dM = mk1(0.f);
+    GP.dA[0] = GP.dA[1] = GP.dA[2] = GP.dM = GP.dR = mk1(0.f);
     if (use_p) GP = disney_eval_grad(V.hd, C, V.dP);
     if (ca)
 #pragma unroll
       for (int j = 0; j < 3; j++) gk[j] = dot(uB, G.dA[j]) + dot(uH, GH.dA[j]) + dot(uP, GP.dA[j]);
     if (dm) gk[4] = 2.2f * powf(V.metal_in, 1.2f) * (dot(uB, G.dM) + dot(uH, GH.dM) + dot(uP, GP.dM));
-  }
-  // roughness: a single-partial dual through the three evaluations
-  if (cr && V.rough_in > 0.f) {
-    D3 alb{dconst(V.hd.albedo.x), dconst(V.hd.albedo.y), dconst(V.hd.albedo.z)};
-    Dual rg = dconst(V.hd.roughness), mt = dconst(V.hd.metallic);
-    rg.d[0] = 2.2f * powf(V.rough_in, 1.2f);
-    D3 Df = disney_eval_d(V.hd, alb, rg, mt, C, V.dir);
-    D3 DfH = disney_eval_d(V.hd, alb, rg, mt, C, V.dH);
-    float acc = wd.x * (kH.x * DfH.x.d[0] + kB.x * Df.x.d[0]) + wd.y * (kH.y * DfH.y.d[0] + kB.y * Df.y.d[0]) +
-                wd.z * (kH.z * DfH.z.d[0] + kB.z * Df.z.d[0]) + ra.x * Df.x.d[0] + ra.y * Df.y.d[0] + ra.z * Df.z.d[0];
-    if (use_p) {
-      D3 DfP = disney_eval_d(V.hd, alb, rg, mt, C, V.dP);
-      acc += wd.x * kP.x * DfP.x.d[0] + wd.y * kP.y * DfP.y.d[0] + wd.z * kP.z * DfP.z.d[0];
-    }
-    gk[3] = acc;
+    if (dr) gk[3] = 2.2f * powf(V.rough_in, 1.2f) * (dot(uB, G.dR) + dot(uH, GH.dR) + dot(uP, GP.dR));
   }
   agg_add<kParams>(g_mat, V.mat, gk);
   if (vH) {
