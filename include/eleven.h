@@ -298,6 +298,13 @@ er_status er_render_paths(er_scene* scene, const er_render_opts* opts,
  * entries; any may be NULL.  Builds the table on first use. */
 er_status er_env_distribution(er_scene* scene, uint32_t* counts, int32_t* alias, uint32_t* thresh);
 
+/* The texel HDRI::binarySearch returns for each of its 2^24 inputs
+ * k * 2^-24, k = 1..2^24 (table[k - 1]); environments of at least 65,536
+ * texels are sampled through this table (one load instead of the search,
+ * same texel).  table: 2^24 int32 (host).  ER_ERR_INVALID_ARG for a smaller
+ * environment, which is sampled by the search itself. */
+er_status er_env_search_table(er_scene* scene, int32_t* table);
+
 /* -------------------------------------------------------------- tangents -- */
 /* Per-corner tangents (9 floats per triangle) and a per-triangle sign in
  * the manner of the MikkTSpace generator the reference's loader runs on

@@ -90,3 +90,51 @@ def test_alias_render_unbiased_against_search():
         # the flag is deterministic
         again = s.render(64, max_depth=3, seed=11, flags=A.ER_RENDER_ENV_ALIAS)["beauty"][:, :3]
         np.testing.assert_array_equal(again, alias)
+
+
+def test_search_lookup_table_matches_the_oracle_per_path():
+    """Environments of >= 65,536 texels are sampled through a table of the
+    CDF search's result for each of its 2^24 inputs (env.cu): the chosen
+    texels, and so the paths, are the reference search's.  Per-path parity
+    with the oracle (which runs the search) on a 512x256 environment, and
+    the film of a second scene handle built the same way is identical."""
+    arrays = scenes.displaced_spheres(20000, 5, 64, 48, 2, env_w=512, env_h=256)
+    scene = _lib.Scene(arrays)
+    orc = O.OrcScene(arrays)
+    rad, b = scene.render_paths(spp=2, max_depth=4, seed=13)
+    rrad, rb = orc.render_paths(spp=2, max_depth=4, seed=13)
+    assert (b == rb).mean() > 0.99
+    close = np.isclose(rad, rrad, rtol=1e-3, atol=1e-5).all(axis=2)
+    both_nan = np.isnan(rad).any(2) & np.isnan(rrad).any(2)
+    assert (close | both_nan).mean() > 0.98
+    a = scene.render(4, max_depth=4, seed=2)["beauty"]
+    other = _lib.Scene(arrays)
+    c = other.render(4, max_depth=4, seed=2)["beauty"]
+    assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+    other.close()
+    scene.close()
+    orc.close()
+
+
+@pytest.mark.parametrize("w,h,sun", [(512, 256, 8), (256, 256, 0)])
+def test_search_table_is_the_search(w, h, sun):
+    """The 2^24-entry table equals the reference search everywhere: it is
+    non-decreasing (as the search is in its input) and its histogram equals
+    the oracle's per-texel counts of the search, so the two maps agree on
+    every input."""
+    arrays = _env_scene(w, h, sun)
+    cdf, _ = O.Probes(O.orc(), "orc_p_").hdri_cdf(arrays.env)
+    want = O.hdri_counts(cdf, w * h)
+    table = np.zeros(1 << 24, np.int32)
+    with _lib.Scene(arrays) as s:
+        _lib.check(_lib.load().er_env_search_table(s.h, _lib._p(table)), "er_env_search_table")
+    assert np.all(np.diff(table) >= 0)
+    assert table.min() >= 0 and table.max() < w * h
+    np.testing.assert_array_equal(np.bincount(table, minlength=w * h), want)
+
+
+def test_search_table_needs_a_large_environment():
+    arrays = _env_scene(64, 32, 0)
+    table = np.zeros(1 << 24, np.int32)
+    with _lib.Scene(arrays) as s:
+        assert _lib.load().er_env_search_table(s.h, _lib._p(table)) == A.ER_ERR_INVALID_ARG

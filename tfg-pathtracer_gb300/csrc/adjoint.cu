@@ -266,11 +266,9 @@ er_status check_replay_opts(er_scene* s, const er_render_opts* o) {
   if (o->flags & ~(uint32_t)(ER_RENDER_DEVICE_OUT | ER_RENDER_ENV_ALIAS))
     return fail(ER_ERR_INVALID_ARG, "only ER_RENDER_DEVICE_OUT and ER_RENDER_ENV_ALIAS apply here");
   ER_CUDA(cudaSetDevice(s->device));
-  if ((o->flags & ER_RENDER_ENV_ALIAS)) {
-    er_status st = build_env_alias(s);
-    if (st != ER_OK) return st;
-  }
-  return ER_OK;
+  er_status st;
+  if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
+  return build_env_lut(s);
 }
 
 WaveParams replay_params(const er_scene* s, const er_render_opts* o) {
@@ -400,8 +398,7 @@ extern "C" er_status er_scene_set_params(er_scene* s, const float* materials, co
                             s->stream));
     ER_CUDA(cudaStreamSynchronize(s->stream));
     s->dev.radiance_sum = rsum;
-    s->dev.alias_idx = nullptr;  // rebuilt on next use
-    s->dev.alias_thresh = nullptr;
+    invalidate_env_tables(s);  // refilled on next use
   }
   return ER_OK;
 }

@@ -535,6 +535,7 @@ extern "C" er_status er_batch_set_jobs(er_batch* b, const er_batch_job* jobs, in
     const er_batch_job& J = jobs[j];
     er_scene* sc = b->scenes[(size_t)J.scene];
     if ((J.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(sc)) != ER_OK) return st;
+    if ((st = build_env_lut(sc)) != ER_OK) return st;
     Film& F = b->films[(size_t)j];
     F.w = J.camera.x_res;
     F.h = J.camera.y_res;
@@ -552,6 +553,7 @@ extern "C" er_status er_batch_set_jobs(er_batch* b, const er_batch_job* jobs, in
     D.cdf = S.cdf;
     D.alias_idx = S.alias_idx;
     D.alias_thresh = S.alias_thresh;
+    D.env_lut = S.env_lut;
     D.lights = S.lights;
     D.radiance_sum = S.radiance_sum;
     D.n_lights = S.n_lights;

@@ -25,6 +25,16 @@ namespace {
 
 constexpr int64_t kGrid = (int64_t)1 << 24;
 
+// The search's texel for each of its 2^24 inputs: a table lookup then
+// returns exactly what the search returns, with one load instead of
+// ~log2(w*h) dependent ones.
+__global__ void k_env_lut(const float* __restrict__ cdf, int32_t n, int32_t* lut) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kGrid) return;
+  float r = (float)(k + 1) * (1.0f / 16777216.0f);  // u01 of (k << 8)
+  lut[k] = hdri_search(cdf, r, n);
+}
+
 __global__ void k_env_counts(const float* __restrict__ cdf, int32_t n, uint32_t* counts) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= kGrid) return;
@@ -42,13 +52,38 @@ __global__ void k_env_weights(const uint32_t* counts, int32_t n, double* q) {
 
 }  // namespace
 
-er_status build_env_alias(er_scene* s) {
-  if (s->dev.alias_idx) return ER_OK;
+void invalidate_env_tables(er_scene* s) {
+  s->env_alias_ok = false;
+  s->env_lut_ok = false;
+  s->dev.alias_idx = nullptr;
+  s->dev.alias_thresh = nullptr;
+  s->dev.env_lut = nullptr;
+}
+
+er_status build_env_lut(er_scene* s) {
   const int32_t n = s->dev.env.w * s->dev.env.h;
-  void *d_counts = nullptr, *d_q = nullptr;
+  if (s->env_lut_ok || n < kEnvLutMinTexels) return ER_OK;
   er_status st;
-  if ((st = dev_alloc(s, &d_counts, (size_t)n * 4)) != ER_OK) return st;
-  if ((st = dev_alloc(s, &d_q, (size_t)n * 8)) != ER_OK) return st;
+  if (!s->env_lut_buf && (st = dev_alloc(s, &s->env_lut_buf, (size_t)kGrid * 4)) != ER_OK) return st;
+  k_env_lut<<<(unsigned)(kGrid / 256), 256, 0, s->stream>>>(s->dev.cdf, n, (int32_t*)s->env_lut_buf);
+  ER_CUDA(cudaGetLastError());
+  s->dev.env_lut = (const int32_t*)s->env_lut_buf;
+  s->env_lut_ok = true;
+  return ER_OK;
+}
+
+er_status build_env_alias(er_scene* s) {
+  if (s->env_alias_ok) return ER_OK;
+  const int32_t n = s->dev.env.w * s->dev.env.h;
+  er_status st;
+  if (!s->env_counts) {
+    void* p = nullptr;
+    if ((st = dev_alloc(s, &p, (size_t)n * 4)) != ER_OK) return st;
+    s->env_counts = (const uint32_t*)p;
+  }
+  if (!s->env_q && (st = dev_alloc(s, &s->env_q, (size_t)n * 8)) != ER_OK) return st;
+  void* d_counts = const_cast<uint32_t*>(s->env_counts);
+  void* d_q = s->env_q;
   ER_CUDA(cudaMemsetAsync(d_counts, 0, (size_t)n * 4, s->stream));
   k_env_counts<<<(unsigned)(kGrid / 256), 256, 0, s->stream>>>(s->dev.cdf, n, (uint32_t*)d_counts);
   k_env_weights<<<(n + 255) / 256, 256, 0, s->stream>>>((const uint32_t*)d_counts, n, (double*)d_q);
@@ -83,19 +118,32 @@ er_status build_env_alias(er_scene* s) {
     // accept the column itself when the 32-bit coin is below p * 2^32
     thresh[(size_t)i] = p >= 1.0 ? 0xFFFFFFFFu : (uint32_t)std::floor(p * 4294967296.0);
   }
-  void *d_alias = nullptr, *d_thr = nullptr;
-  if ((st = upload(s, &d_alias, alias.data(), (size_t)n * 4)) != ER_OK) return st;
-  if ((st = upload(s, &d_thr, thresh.data(), (size_t)n * 4)) != ER_OK) return st;
+  if (!s->env_alias_buf && (st = dev_alloc(s, &s->env_alias_buf, (size_t)n * 4)) != ER_OK) return st;
+  if (!s->env_thresh_buf && (st = dev_alloc(s, &s->env_thresh_buf, (size_t)n * 4)) != ER_OK) return st;
+  ER_CUDA(cudaMemcpyAsync(s->env_alias_buf, alias.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+  ER_CUDA(cudaMemcpyAsync(s->env_thresh_buf, thresh.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
   ER_CUDA(cudaStreamSynchronize(s->stream));
-  s->dev.alias_idx = (const int32_t*)d_alias;
-  s->dev.alias_thresh = (const uint32_t*)d_thr;
-  s->env_counts = (const uint32_t*)d_counts;
+  s->dev.alias_idx = (const int32_t*)s->env_alias_buf;
+  s->dev.alias_thresh = (const uint32_t*)s->env_thresh_buf;
+  s->env_alias_ok = true;
   return ER_OK;
 }
 
 }  // namespace er
 
 using namespace er;
+
+extern "C" er_status er_env_search_table(er_scene* s, int32_t* table) {
+  if (!s || !table) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+  ER_CUDA(cudaSetDevice(s->device));
+  if ((int64_t)s->dev.env.w * s->dev.env.h < kEnvLutMinTexels)
+    return fail(ER_ERR_INVALID_ARG, "environment below the table threshold: sampled by the search");
+  er_status st = build_env_lut(s);
+  if (st != ER_OK) return st;
+  ER_CUDA(cudaMemcpyAsync(table, s->env_lut_buf, (size_t)kGrid * 4, cudaMemcpyDeviceToHost, s->stream));
+  ER_CUDA(cudaStreamSynchronize(s->stream));
+  return ER_OK;
+}
 
 extern "C" er_status er_env_distribution(er_scene* s, uint32_t* counts, int32_t* alias, uint32_t* thresh) {
   if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");

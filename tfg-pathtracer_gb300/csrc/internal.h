@@ -135,6 +135,7 @@ struct DevScene {
   const float* cdf;      // env CDF, w*h+1 floats (HDRI.hpp:107-128)
   const int32_t* alias_idx;   // env alias table (w*h) or null (env.cu)
   const uint32_t* alias_thresh;
+  const int32_t* env_lut;     // the CDF search's texel for each of its 2^24 inputs, or null (env.cu)
   float radiance_sum;
   int32_t n_lights;
   int32_t n_mats;
@@ -187,6 +188,7 @@ struct BatchJobDev {
   const float* cdf;
   const int32_t* alias_idx;
   const uint32_t* alias_thresh;
+  const int32_t* env_lut;
   const er_point_light* lights;
   float radiance_sum;
   int32_t n_lights;
@@ -261,7 +263,14 @@ struct er_scene {
   unsigned long long* d_stats = nullptr;  // device ray counters
   std::vector<cudaEvent_t> ev_pool;       // per-launch profiling events
   std::vector<int> ev_stage;
-  const uint32_t* env_counts = nullptr;   // effective env texel counts (env.cu)
+  // environment tables (env.cu): allocated once, refilled after an
+  // environment change
+  const uint32_t* env_counts = nullptr;   // effective env texel counts
+  void* env_q = nullptr;                  // FP64 alias weights
+  void* env_alias_buf = nullptr;
+  void* env_thresh_buf = nullptr;
+  void* env_lut_buf = nullptr;
+  bool env_alias_ok = false, env_lut_ok = false;
   int64_t texel_count = 0;                // float4 entries of dev.texels (textures + env)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // progressive readback (er_snapshot): a copy of the film after each wave
@@ -282,6 +291,11 @@ void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
 er_status build_env_alias(er_scene* s);
+// The search lookup table for environments of at least kEnvLutMinTexels
+// texels (no-op below); the tables are refilled after invalidate_env_tables.
+er_status build_env_lut(er_scene* s);
+void invalidate_env_tables(er_scene* s);
+constexpr int64_t kEnvLutMinTexels = 65536;
 // Per-corner tangents and per-triangle signs (tangents.cpp).
 void compute_tangents(int64_t n_tris, const float* pos, const float* nrm, const float* uv, float* tangents,
                       float* sign);

@@ -347,6 +347,7 @@ __global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
         S.cdf = J.cdf;
         S.alias_idx = J.alias_idx;
         S.alias_thresh = J.alias_thresh;
+        S.env_lut = J.env_lut;
         S.lights = J.lights;
         S.radiance_sum = J.radiance_sum;
         S.n_lights = J.n_lights;
@@ -1050,6 +1051,7 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
   const bool aov = o->flags & ER_RENDER_AOV;
   const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
   if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
+  if ((st = build_env_lut(s)) != ER_OK) return st;
   if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
   if ((o->flags & ER_RENDER_SNAPSHOTS) && (st = ensure_snapshot(s)) != ER_OK) return st;
   const bool keep = o->flags & ER_RENDER_KEEP_PATHS;
@@ -1132,7 +1134,7 @@ extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float
   }
   er_render_opts oo = *o;
   oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
-  if ((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) {
+  if (((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) || (st = build_env_lut(s)) != ER_OK) {
     cudaFree(d_rad);
     cudaFree(d_b);
     return st;

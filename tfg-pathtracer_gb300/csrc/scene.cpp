@@ -362,6 +362,7 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
   S.cdf = (const float*)p_cdf;
   S.alias_idx = nullptr;
   S.alias_thresh = nullptr;
+  S.env_lut = nullptr;
   S.radiance_sum = rsum;
   S.n_lights = d->light_count;
   S.n_mats = d->material_count;

@@ -130,6 +130,8 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
     uint32_t coin = philox(make_uint4(idx, sample, 2u + (uint32_t)bounce, 1u), k0, k1).x;
     int32_t col = (int32_t)__umulhi(rn.w, (uint32_t)(E.w * E.h));
     cnt = coin < __ldg(S.alias_thresh + col) ? col : __ldg(S.alias_idx + col);
+  } else if (S.env_lut) {
+    cnt = __ldg(S.env_lut + (rn.w >> 8));  // == hdri_search(S.cdf, r1, w*h): r1 = u01(rn.w)
   } else {
     cnt = hdri_search(S.cdf, r1, E.w * E.h);
   }

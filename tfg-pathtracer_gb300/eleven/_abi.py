@@ -175,6 +175,7 @@ EXPORTED = [
     "er_scene_create", "er_scene_load", "er_scene_info_get",
     "er_scene_set_camera", "er_scene_get_camera", "er_scene_free",
     "er_render", "er_film_read", "er_snapshot", "er_render_paths", "er_render_noalloc", "er_env_distribution",
+    "er_env_search_table",
     "er_scene_get_params", "er_scene_set_params", "er_render_replay", "er_backward",
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",

@@ -65,6 +65,8 @@ def load(build_if_missing=True):
     L.er_snapshot.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_env_distribution.restype = A.er_status
     L.er_env_distribution.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.er_env_search_table.restype = A.er_status
+    L.er_env_search_table.argtypes = [C.c_void_p, C.c_void_p]
     L.er_render_noalloc.restype = A.er_status
     L.er_render_noalloc.argtypes = [C.c_void_p, C.POINTER(A.er_render_opts), C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_render_paths.restype = A.er_status
