@@ -263,6 +263,12 @@ __global__ void __launch_bounds__(kTravBlock, kTravMinBlocks)
   }
 }
 
+// Every channel of t has the bits of o.
+__device__ __forceinline__ bool same_bits3(f3 t, float o) {
+  const uint32_t b = __float_as_uint(o);
+  return __float_as_uint(t.x) == b && __float_as_uint(t.y) == b && __float_as_uint(t.z) == b;
+}
+
 // Resolve the pending MIS terms of a path's last shaded vertex
 // (kernel.cu:351-355,433): light += reduction * ((w1*H + w2*P) + w3*B),
 // with an occluded strategy contributing w*0 (NaN when its weight is).
@@ -387,17 +393,26 @@ __global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
         }
         env_o = V.env_o;
         env_d = V.env_d;
-        push_env = true;
+        // A shadow ray whose strategy term is bitwise the same visible or
+        // occluded (w * H == w * 0 in every channel: the BRDF is zero
+        // towards the light, e.g. it lies below the surface) cannot change
+        // the film, so it is not traced; its visibility is set to "visible".
+        // The gradient pass traces every ray (its env-texel derivative
+        // depends on visibility even where the radiance term is zero).
+        const float oH = V.w1 * 0.0f, oP = V.w2 * 0.0f;
+        push_env = GRAD || !same_bits3(V.tH, oH);
+        if (!push_env) w.vis[2 * (size_t)p] = 1;
         if (V.has_pt) {
           pt_o = V.pt_o;
           pt_d = V.pt_d;
           pt_p = V.pos;
           pt_dist = V.dist;
-          push_pt = true;
+          push_pt = GRAD || !same_bits3(V.tP, oP);
+          if (!push_pt) w.vis[2 * (size_t)p + 1] = 1;
         }
-        uint32_t fl = 1u | (push_pt ? 2u : 0u);
-        w.pend[4 * (size_t)p] = make_float4(V.tH.x, V.tH.y, V.tH.z, V.w1 * 0.0f);
-        w.pend[4 * (size_t)p + 1] = make_float4(V.tP.x, V.tP.y, V.tP.z, V.w2 * 0.0f);
+        uint32_t fl = 1u | (V.has_pt ? 2u : 0u);
+        w.pend[4 * (size_t)p] = make_float4(V.tH.x, V.tH.y, V.tH.z, oH);
+        w.pend[4 * (size_t)p + 1] = make_float4(V.tP.x, V.tP.y, V.tP.z, oP);
         w.pend[4 * (size_t)p + 2] = make_float4(V.tB.x, V.tB.y, V.tB.z, __uint_as_float(fl));
         w.pend[4 * (size_t)p + 3] = make_float4(thr.x, thr.y, thr.z, 0.f);
         thr = mk(__fmul_rn(thr.x, V.g.x), __fmul_rn(thr.y, V.g.y), __fmul_rn(thr.z, V.g.z));
