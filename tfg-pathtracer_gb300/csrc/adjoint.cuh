@@ -36,7 +36,7 @@ struct EvalGrad {
 __device__ __forceinline__ EvalGrad disney_eval_grad(const HitData& hd, const DisneyCtx& c, f3 L) {
   EvalGrad g;
   g.dA[0] = g.dA[1] = g.dA[2] = g.dM = g.dR = mk1(0.f);
-  if (!(hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f)) return g;
+  if (!disney_gate(hd, c, L)) return g;
   const f3 H = normalized(L + c.V);
   const float NDotL = fabsf(dot(c.N, L));
   const float NDotV = fabsf(dot(c.N, c.V));

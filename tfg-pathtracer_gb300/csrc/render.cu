@@ -397,17 +397,18 @@ __global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
         // occluded (w * H == w * 0 in every channel: the BRDF is zero
         // towards the light, e.g. it lies below the surface) cannot change
         // the film, so it is not traced; its visibility is set to "visible".
-        // The gradient pass traces every ray (its env-texel derivative
-        // depends on visibility even where the radiance term is zero).
+        // The gradient pass also needs the BRDF's partials to vanish there,
+        // which holds where DisneyEval's own gate rejects the direction (its
+        // env-texel derivative depends on visibility wherever f is not 0).
         const float oH = V.w1 * 0.0f, oP = V.w2 * 0.0f;
-        push_env = GRAD || !same_bits3(V.tH, oH);
+        push_env = !same_bits3(V.tH, oH) || (GRAD && disney_gate(V.hd, V.C, V.dH));
         if (!push_env) w.vis[2 * (size_t)p] = 1;
         if (V.has_pt) {
           pt_o = V.pt_o;
           pt_d = V.pt_d;
           pt_p = V.pos;
           pt_dist = V.dist;
-          push_pt = GRAD || !same_bits3(V.tP, oP);
+          push_pt = !same_bits3(V.tP, oP) || (GRAD && disney_gate(V.hd, V.C, V.dP));
           if (!push_pt) w.vis[2 * (size_t)p + 1] = 1;
         }
         uint32_t fl = 1u | (V.has_pt ? 2u : 0u);

@@ -154,10 +154,16 @@ __device__ __forceinline__ f3 disney_sample(const HitData& hd, const DisneyCtx& 
   return v - H * (2.0f * dot(v, H));
 }
 
+// DisneyEval's condition for a non-zero value (Disney.hpp:200): outside it
+// the value and every partial are zero.
+__device__ __forceinline__ bool disney_gate(const HitData& hd, const DisneyCtx& c, f3 L) {
+  return hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f;
+}
+
 // Disney.hpp:179-253
 __device__ __forceinline__ f3 disney_eval(const HitData& hd, const DisneyCtx& c, f3 L) {
   f3 brdf = mk1(0.0f);
-  if (hd.transmission < 1.0f && dot(c.N, L) > 0.0f && dot(c.N, c.V) > 0.0f) {
+  if (disney_gate(hd, c, L)) {
     f3 H = normalized(L + c.V);
     float NDotL = fabsf(dot(c.N, L));
     float NDotV = fabsf(dot(c.N, c.V));
