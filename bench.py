@@ -158,6 +158,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def host_buffers(npix):
+    """Film readback buffers in page-locked host memory (torch's pinned
+    allocator), else pageable numpy arrays; returns the kind as well."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            b = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
+            s = torch.empty((npix,), dtype=torch.int32, pin_memory=True)
+            c = torch.empty((npix,), dtype=torch.int32, pin_memory=True)
+            return b.numpy(), s.numpy().view(np.uint32), c.numpy().view(np.uint32), "pinned"
+    except Exception:
+        pass
+    return (np.zeros((npix, 4), np.float32), np.zeros(npix, np.uint32), np.zeros(npix, np.uint32), "pageable")
+
+
 def traffic_per_ray():
     """DRAM bytes per traced ray of the dominant kernel from the committed ncu
     summary (profiles/extend_c1_dram.json), or None."""
@@ -268,10 +283,9 @@ def run_gpu(args):
     pst = scene.render(spp=prof_steps, max_depth=max_depth, sample_begin=base + 1 + args.warmup,
                        flags=A.ER_RENDER_NO_OUTPUT | A.ER_RENDER_PROFILE | env_flag)["stats"]
 
-    # e2e through the C-ABI with host buffers, one 1-spp call per step
-    beauty = np.zeros((npix, 4), np.float32)
-    samples = np.zeros(npix, np.uint32)
-    pathcount = np.zeros(npix, np.uint32)
+    # e2e through the C-ABI with host buffers (page-locked, as a caller
+    # that reads the film every step allocates them), one 1-spp call per step
+    beauty, samples, pathcount, host_mem = host_buffers(npix)
     import ctypes as C
     L = _lib.load()
     o = A.er_render_opts(1, 0, max_depth, 0, 0, 0, 0)
@@ -310,7 +324,7 @@ def run_gpu(args):
                        triangles=arrays.tri_count,
                        l2="working set > 126 MB L2 (no flush)", parallelism="replicas" if world > 1 else "1 GPU"),
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(C.sizeof(A.er_render_opts)),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "host_memory": host_mem},
         "gpu_launches": int(st.kernel_launches),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),

@@ -26,7 +26,10 @@ namespace er {
 
 enum TraceMode { kClosest = 0, kAny = 1, kPoint = 2 };
 
-constexpr int kTravBlock = 128;
+#ifndef ER_TRAV_BLOCK
+#define ER_TRAV_BLOCK 128
+#endif
+constexpr int kTravBlock = ER_TRAV_BLOCK;  // threads per traversal block
 #ifndef ER_TRAV_MIN_BLOCKS
 #define ER_TRAV_MIN_BLOCKS 7
 #endif
