@@ -387,7 +387,7 @@ typedef struct er_batch_job {
 
 /* Schedule of a batch render (what er_batch_autotune searches). */
 typedef struct er_batch_tuning {
-  int32_t wave_paths;           /* paths per wave; 0 = 4,194,304; at least the largest job's pixels */
+  int32_t wave_paths;           /* paths per wave; 0 = 8,388,608; at least the largest job's pixels */
   int32_t trace_blocks_per_sm;  /* persistent traversal grid = SMs x this; 0 = as many as fit */
   int32_t shade_blocks_per_sm;  /* shading grid = SMs x this; 0 = as many as fit */
   int32_t split_trace;          /* 1: extension, point-light and env rays as three traversal launches */

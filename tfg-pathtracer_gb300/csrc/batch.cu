@@ -64,7 +64,7 @@ struct er_batch {
 
 namespace {
 
-constexpr int32_t kDefaultWavePaths = 1 << 22;
+constexpr int32_t kDefaultWavePaths = 1 << 23;
 
 er_status balloc(er_batch* b, void** p, size_t bytes) {
   *p = nullptr;
@@ -656,7 +656,7 @@ extern "C" er_status er_batch_autotune(er_batch* b, int32_t reps, er_batch_tunin
     return ER_OK;
   };
   if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.wave_paths = v; },
-                     {1 << 20, 1 << 21, 1 << 22, 1 << 23})) != ER_OK)
+                     {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24})) != ER_OK)
     return st;
   if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.trace_blocks_per_sm = v; }, {0, 4, 5, 6})) != ER_OK)
     return st;
