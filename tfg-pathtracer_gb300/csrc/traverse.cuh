@@ -248,7 +248,9 @@ struct Traverser {
       done = true;
       return;
     }
-    float4 nx, fx, ny, fy, nz, fz, dl;
+    // slab distances of the four children: near / far plane per axis
+    float tnx[4], tny[4], tnz[4], tfx[4], tfy[4], tfz[4];
+    float4 dl;
     int4 ch;
     if (Q8) {
       const uint4* qn = S.qnodes + 4 * (size_t)node;
@@ -259,28 +261,64 @@ struct Traverser {
       uint32_t qnx = (sgn & 1u) ? b.y : b.x, qfx = (sgn & 1u) ? b.x : b.y;
       uint32_t qny = (sgn & 2u) ? b.w : b.z, qfy = (sgn & 2u) ? b.z : b.w;
       uint32_t qnz = (sgn & 4u) ? c.y : c.x, qfz = (sgn & 4u) ? c.x : c.y;
-      nx = make_float4(q8_plane(ox, qnx, 0, sx), q8_plane(ox, qnx, 1, sx), q8_plane(ox, qnx, 2, sx), q8_plane(ox, qnx, 3, sx));
-      fx = make_float4(q8_plane(ox, qfx, 0, sx), q8_plane(ox, qfx, 1, sx), q8_plane(ox, qfx, 2, sx), q8_plane(ox, qfx, 3, sx));
-      ny = make_float4(q8_plane(oy, qny, 0, sy), q8_plane(oy, qny, 1, sy), q8_plane(oy, qny, 2, sy), q8_plane(oy, qny, 3, sy));
-      fy = make_float4(q8_plane(oy, qfy, 0, sy), q8_plane(oy, qfy, 1, sy), q8_plane(oy, qfy, 2, sy), q8_plane(oy, qfy, 3, sy));
-      nz = make_float4(q8_plane(oz, qnz, 0, sz), q8_plane(oz, qnz, 1, sz), q8_plane(oz, qnz, 2, sz), q8_plane(oz, qnz, 3, sz));
-      fz = make_float4(q8_plane(oz, qfz, 0, sz), q8_plane(oz, qfz, 1, sz), q8_plane(oz, qfz, 2, sz), q8_plane(oz, qfz, 3, sz));
+      // The decode folded into the slab: (o + q s) inv + bias =
+      // q (s inv) + (o inv + bias), with s inv exact (s a power of two) and
+      // one rounding each for o inv + bias and the final fma.  Their error
+      // is below 2^-24 |inv| (3 extent + 2 |origin|), inside the bias
+      // widening (8x 2^-24 |inv| (extent + |origin|)), which therefore also
+      // covers the difference between the exact o + q s and its float the
+      // builder checked against the FP32 box.  An s inv that overflows
+      // (node extents beyond 2^35) takes the plain decode.
+      const float Ax = sx * inv.x, Ay = sy * inv.y, Az = sz * inv.z;
+      if (fabsf(Ax) < INFINITY && fabsf(Ay) < INFINITY && fabsf(Az) < INFINITY) {
+        const float Bnx = fmaf(ox, inv.x, bnear.x), Bfx = fmaf(ox, inv.x, bfar.x);
+        const float Bny = fmaf(oy, inv.y, bnear.y), Bfy = fmaf(oy, inv.y, bfar.y);
+        const float Bnz = fmaf(oz, inv.z, bnear.z), Bfz = fmaf(oz, inv.z, bfar.z);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          tnx[k] = fmaf(byte_of(qnx, k), Ax, Bnx);
+          tfx[k] = fmaf(byte_of(qfx, k), Ax, Bfx);
+          tny[k] = fmaf(byte_of(qny, k), Ay, Bny);
+          tfy[k] = fmaf(byte_of(qfy, k), Ay, Bfy);
+          tnz[k] = fmaf(byte_of(qnz, k), Az, Bnz);
+          tfz[k] = fmaf(byte_of(qfz, k), Az, Bfz);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          tnx[k] = fmaf(q8_plane(ox, qnx, k, sx), inv.x, bnear.x);
+          tfx[k] = fmaf(q8_plane(ox, qfx, k, sx), inv.x, bfar.x);
+          tny[k] = fmaf(q8_plane(oy, qny, k, sy), inv.y, bnear.y);
+          tfy[k] = fmaf(q8_plane(oy, qfy, k, sy), inv.y, bfar.y);
+          tnz[k] = fmaf(q8_plane(oz, qnz, k, sz), inv.z, bnear.z);
+          tfz[k] = fmaf(q8_plane(oz, qfz, k, sz), inv.z, bfar.z);
+        }
+      }
       ch = make_int4((int)c.z, (int)c.w, (int)e.x, (int)e.y);
       float dd = __uint_as_float(e.z);
       dl = make_float4(dd, dd, dd, dd);
     } else {
       const float4* nd = S.nodes + 8 * (size_t)node;
-      nx = __ldg(nd + (sgn & 1u)); fx = __ldg(nd + 1 - (sgn & 1u));
-      ny = __ldg(nd + 2 + ((sgn >> 1) & 1u)); fy = __ldg(nd + 3 - ((sgn >> 1) & 1u));
-      nz = __ldg(nd + 4 + ((sgn >> 2) & 1u)); fz = __ldg(nd + 5 - ((sgn >> 2) & 1u));
+      const float4 nx = __ldg(nd + (sgn & 1u)), fx = __ldg(nd + 1 - (sgn & 1u));
+      const float4 ny = __ldg(nd + 2 + ((sgn >> 1) & 1u)), fy = __ldg(nd + 3 - ((sgn >> 1) & 1u));
+      const float4 nz = __ldg(nd + 4 + ((sgn >> 2) & 1u)), fz = __ldg(nd + 5 - ((sgn >> 2) & 1u));
       float4 c4 = __ldg(nd + 6);
       ch = make_int4(__float_as_int(c4.x), __float_as_int(c4.y), __float_as_int(c4.z), __float_as_int(c4.w));
       dl = __ldg(nd + 7);
+      const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
+      const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
+      const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        tnx[k] = fmaf(nxa[k], inv.x, bnear.x);
+        tfx[k] = fmaf(fxa[k], inv.x, bfar.x);
+        tny[k] = fmaf(nya[k], inv.y, bnear.y);
+        tfy[k] = fmaf(fya[k], inv.y, bfar.y);
+        tnz[k] = fmaf(nza[k], inv.z, bnear.z);
+        tfz[k] = fmaf(fza[k], inv.z, bfar.z);
+      }
     }
     if (STATS) { st.nodes++; st.boxes += 4; }
-    const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
-    const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
-    const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
     const float dla[4] = {dl.x, dl.y, dl.z, dl.w};
     const int32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
     const float lim = limit() * 1.000001f + slack;
@@ -288,8 +326,8 @@ struct Traverser {
     int32_t ic[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      float tnear = max3f(fmaf(nxa[c], inv.x, bnear.x), fmaf(nya[c], inv.y, bnear.y), fmaf(nza[c], inv.z, bnear.z));
-      float tfar = min3f(fmaf(fxa[c], inv.x, bfar.x), fmaf(fya[c], inv.y, bfar.y), fmaf(fza[c], inv.z, bfar.z));
+      float tnear = max3f(tnx[c], tny[c], tnz[c]);
+      float tfar = min3f(tfx[c], tfy[c], tfz[c]);
       // FP32 nodes reject empty slots by their inverted boxes; a Q8 empty
       // slot decodes to an inverted box too, but the bias widening could
       // reopen it on a tiny node, so it is checked
