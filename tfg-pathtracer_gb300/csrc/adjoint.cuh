@@ -133,53 +133,84 @@ __device__ __forceinline__ void agg_add(float* base, int64_t key, float (&v)[N])
 }
 
 // Gradient contributions of one shaded vertex (the detached estimator of
-// adjoint.cu): thr = path throughput before the vertex, dl = d loss / d
-// sample radiance, (Lx, Ly, Lz) = radiance gathered up to and including
-// this vertex, Lt = the sample's total radiance, vH / vP = visibility of
-// the env and point-light shadow rays.  Material gradients go to
-// g_mat[5 * material + k] (global or shared memory), env gradients to
-// g_env[3 * texel + c].
-__device__ __forceinline__ void vertex_gradient(const DevScene& S, const VertexShade& V, f3 thr, f3 dl, f3 Lt,
-                                                float Lx, float Ly, float Lz, bool vH, bool vP, float* g_mat,
-                                                float* g_env) {
+// adjoint.cu), prepared when the vertex is shaded and applied when its
+// shadow rays have been traced.  With thr = path throughput before the
+// vertex, dl = d loss / d sample radiance, Lt = the sample's total radiance
+// and Lb = the radiance gathered before the vertex, the strategy terms
+// resolve to L = Lb + thr (h + p + tB) (h = tH visible, w1*0 occluded; p
+// alike), and the derivative of the radiance still to come, Lt - L,
+// through the vertex's BRDF f is (Lt - L) df / f per channel.  Every
+// parameter's derivative is therefore affine in the two visibility bits:
+//   g = K0 + vH dH + vP dP,
+// with K0 taken at vH = vP = 0.  The coefficients are stored per path
+// (5 float4: K0, dH, dP for the 5 material parameters, the material slot
+// or -1 when the sample has no adjoint, the env-texel gradient and texel)
+// and apply_vertex_gradient adds g to g_mat[5 * material + k] and, when the
+// env ray was visible, the texel's to g_env[3 * texel + c].
+__device__ __forceinline__ void vertex_grad_coeffs(const DevScene& S, const VertexShade& V, f3 thr, f3 dl, f3 Lt,
+                                                   f3 Lb, float4* out) {
+  if (dl.x == 0.f && dl.y == 0.f && dl.z == 0.f) {
+    out[3] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    return;
+  }
   const DevMaterial& M = S.mats[V.mat];
   const f3 f = V.f, fH = V.fH, eH = V.eH;
   const bool ca = M.albedo_tex < 0, cr = M.roughness_tex < 0, cm = M.metallic_tex < 0;
+  const bool dm = cm && V.metal_in > 0.f, dr = cr && V.rough_in > 0.f;
   const DisneyCtx& C = V.C;
   // strategy weights per channel: C_c = thr_c * (kH_c fH_c + kP_c fP_c + kB_c f_c)
-  const f3 kH = vH ? eH * (V.cosH / V.hdriPdf * V.w1) : mk1(0.f);
+  const f3 kH = eH * (V.cosH / V.hdriPdf * V.w1);
   const f3 kB = V.hd.emission * (V.ndl / V.brdfPdf * V.w3);
-  const f3 kP = (V.has_pt && vP) ? V.plv * (V.cosP / V.pointPdf * V.w2) : mk1(0.f);
+  const f3 kP = V.has_pt ? V.plv * (V.cosP / V.pointPdf * V.w2) : mk1(0.f);
   const f3 wd = mk(dl.x * thr.x, dl.y * thr.y, dl.z * thr.z);
-  // radiance still to come carries f through the throughput
-  const f3 La = mk(Lt.x - Lx, Lt.y - Ly, Lt.z - Lz);
-  const f3 ra = mk(f.x != 0.f ? dl.x * La.x / f.x : 0.f, f.y != 0.f ? dl.y * La.y / f.y : 0.f,
-                   f.z != 0.f ? dl.z * La.z / f.z : 0.f);
-  // closed-form partials of the three evaluations
-  float gk[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  const bool use_p = V.has_pt && vP;
-  const bool dm = cm && V.metal_in > 0.f;
-  const bool dr = cr && V.rough_in > 0.f;
+  // (Lt - L) / f split into its visibility-free part and the h, p parts
+  const float oH = V.w1 * 0.0f, oP = V.w2 * 0.0f;
+  const f3 q = mk(f.x != 0.f ? dl.x / f.x : 0.f, f.y != 0.f ? dl.y / f.y : 0.f, f.z != 0.f ? dl.z / f.z : 0.f);
+  const f3 r0 = mk(q.x * (Lt.x - Lb.x - thr.x * (V.tB.x + oH + oP)), q.y * (Lt.y - Lb.y - thr.y * (V.tB.y + oH + oP)),
+                   q.z * (Lt.z - Lb.z - thr.z * (V.tB.z + oH + oP)));
+  const f3 rH = mk(-q.x * thr.x * (V.tH.x - oH), -q.y * thr.y * (V.tH.y - oH), -q.z * thr.z * (V.tH.z - oH));
+  const f3 rP = mk(-q.x * thr.x * (V.tP.x - oP), -q.y * thr.y * (V.tP.y - oP), -q.z * thr.z * (V.tP.z - oP));
+  float k0[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f}, kh[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f},
+        kp[kParams] = {0.f, 0.f, 0.f, 0.f, 0.f};
   if (ca || dm || dr) {
-    const f3 uB = mk(wd.x * kB.x + ra.x, wd.y * kB.y + ra.y, wd.z * kB.z + ra.z);
+    const f3 uB = mk(wd.x * kB.x + r0.x, wd.y * kB.y + r0.y, wd.z * kB.z + r0.z);
     const f3 uH = mk(wd.x * kH.x, wd.y * kH.y, wd.z * kH.z);
     const f3 uP = mk(wd.x * kP.x, wd.y * kP.y, wd.z * kP.z);
     const EvalGrad G = disney_eval_grad(V.hd, C, V.dir);
     const EvalGrad GH = disney_eval_grad(V.hd, C, V.dH);
     EvalGrad GP;
     GP.dA[0] = GP.dA[1] = GP.dA[2] = GP.dM = GP.dR = mk1(0.f);
-    if (use_p) GP = disney_eval_grad(V.hd, C, V.dP);
+    if (V.has_pt) GP = disney_eval_grad(V.hd, C, V.dP);
+    auto put = [&](int k, f3 g, f3 gh, f3 gp, float chain) {
+      k0[k] = chain * dot(uB, g);
+      kh[k] = chain * (dot(rH, g) + dot(uH, gh));
+      kp[k] = chain * (dot(rP, g) + dot(uP, gp));
+    };
     if (ca)
 #pragma unroll
-      for (int j = 0; j < 3; j++) gk[j] = dot(uB, G.dA[j]) + dot(uH, GH.dA[j]) + dot(uP, GP.dA[j]);
-    if (dm) gk[4] = 2.2f * powf(V.metal_in, 1.2f) * (dot(uB, G.dM) + dot(uH, GH.dM) + dot(uP, GP.dM));
-    if (dr) gk[3] = 2.2f * powf(V.rough_in, 1.2f) * (dot(uB, G.dR) + dot(uH, GH.dR) + dot(uP, GP.dR));
+      for (int j = 0; j < 3; j++) put(j, G.dA[j], GH.dA[j], GP.dA[j], 1.0f);
+    if (dr) put(3, G.dR, GH.dR, GP.dR, 2.2f * powf(V.rough_in, 1.2f));
+    if (dm) put(4, G.dM, GH.dM, GP.dM, 2.2f * powf(V.metal_in, 1.2f));
   }
-  agg_add<kParams>(g_mat, V.mat, gk);
+  const float sH = V.cosH / V.hdriPdf * V.w1;
+  out[0] = make_float4(k0[0], k0[1], k0[2], k0[3]);
+  out[1] = make_float4(k0[4], kh[0], kh[1], kh[2]);
+  out[2] = make_float4(kh[3], kh[4], kp[0], kp[1]);
+  out[3] = make_float4(kp[2], kp[3], kp[4], __int_as_float(V.mat));
+  out[4] = make_float4(wd.x * fH.x * sH, wd.y * fH.y * sH, wd.z * fH.z * sH, __int_as_float((int32_t)V.env_texel));
+}
+
+__device__ __forceinline__ void apply_vertex_gradient(const float4* c, bool vH, bool vP, float* g_mat, float* g_env) {
+  const int32_t mat = __float_as_int(c[3].w);
+  if (mat < 0) return;
+  const float h = vH ? 1.f : 0.f, p = vP ? 1.f : 0.f;
+  float gk[kParams] = {c[0].x + h * c[1].y + p * c[2].z, c[0].y + h * c[1].z + p * c[2].w,
+                       c[0].z + h * c[1].w + p * c[3].x, c[0].w + h * c[2].x + p * c[3].y,
+                       c[1].x + h * c[2].y + p * c[3].z};
+  agg_add<kParams>(g_mat, mat, gk);
   if (vH) {
-    float s = V.cosH / V.hdriPdf * V.w1;
-    float ge[3] = {wd.x * fH.x * s, wd.y * fH.y * s, wd.z * fH.z * s};
-    agg_add<3>(g_env, V.env_texel, ge);
+    float ge[3] = {c[4].x, c[4].y, c[4].z};
+    agg_add<3>(g_env, __float_as_int(c[4].w), ge);
   }
 }
 

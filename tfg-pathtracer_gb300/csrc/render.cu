@@ -36,9 +36,7 @@ struct WaveView {
   // adjoint, and the last shaded vertex (origin|slot, direction|bounce, t u v)
   float4* g_lt = nullptr;
   float4* g_dl = nullptr;
-  float4* g_vo = nullptr;
-  float4* g_vd = nullptr;
-  float4* g_vh = nullptr;
+  float4* g_k = nullptr;  // 5 float4 per path: the last vertex's gradient coefficients
   float4* q_o[2] = {nullptr, nullptr};
   float4* q_d[2] = {nullptr, nullptr};
   float4* hits = nullptr;
@@ -289,38 +287,33 @@ __device__ __forceinline__ void resolve(const WaveView& w, int32_t p, float4& L)
   w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
 }
 
-// Gradient of the vertex whose MIS terms were just resolved (L includes
-// them): the vertex is shaded again from its stored hit, with the
-// visibility its shadow rays found.  fl = the pending flags before resolve.
-__device__ __forceinline__ void grad_prev_vertex(const DevScene& S, const WaveParams& P, const WaveView& w,
-                                                 const GradArgs& G, int32_t p, int32_t local, uint32_t fl,
-                                                 float4 L) {
-  const float4 dl4 = w.g_dl[p];
-  if (dl4.x == 0.f && dl4.y == 0.f && dl4.z == 0.f) return;
-  const float4 vo = w.g_vo[p], vd = w.g_vd[p], vh = w.g_vh[p], lt = w.g_lt[p];
-  const int32_t pix = local % P.npix, s = local / P.npix;
-  const uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
-  VertexShade V;
-  shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), __float_as_int(vd.w),
-               mk(vo.x, vo.y, vo.z), mk(vd.x, vd.y, vd.z), vh.x, vh.y, vh.z, __float_as_int(vo.w), V);
-  const float4 rp = w.pend[4 * (size_t)p + 3];
+// Gradient of the vertex whose MIS terms were just resolved: its stored
+// coefficients with the visibility its shadow rays found.  fl = the pending
+// flags before resolve.
+__device__ __forceinline__ void grad_prev_vertex(const WaveView& w, const GradArgs& G, int32_t p, uint32_t fl) {
   const bool vH = w.vis[2 * (size_t)p] != 0;
   const bool vP = (fl & 2u) ? (w.vis[2 * (size_t)p + 1] != 0) : true;
-  vertex_gradient(S, V, mk(rp.x, rp.y, rp.z), mk(dl4.x, dl4.y, dl4.z), mk(lt.x, lt.y, lt.z), L.x, L.y, L.z, vH, vP,
-                  G.g_mat, G.g_env);
+  apply_vertex_gradient(w.g_k + 5 * (size_t)p, vH, vP, G.g_mat, G.g_env);
 }
 
 #ifndef ER_SHADE_MIN_BLOCKS
-#define ER_SHADE_MIN_BLOCKS 6
+#define ER_SHADE_MIN_BLOCKS 7
 #endif
-// Resident 128-thread shade blocks per SM the register budget is sized for
-// (85 registers; unbounded the kernel takes 117 and 4 blocks, and the
-// latency of its texture / CDF loads is poorly hidden: 10 % longer on the
-// 1080p scene).  The gradient variant keeps its full budget.
+#ifndef ER_SHADE_GRAD_MIN_BLOCKS
+#define ER_SHADE_GRAD_MIN_BLOCKS 12
+#endif
+// Resident 128-thread shade blocks per SM the register budgets are sized
+// for.  Both kernels wait on dependent loads (texture, material, env
+// lookups, atomics), so occupancy pays for some spilling.  Forward: 73
+// registers at 7 blocks (unbounded 117 at 4 blocks: 10 % longer stage on
+// the 1080p scene; 8 blocks spill too much).  Gradient: 42 registers at 12
+// blocks (unbounded 209 at 2 blocks): backward of the 512x512 adjoint
+// workload 34.9 vs 49.7 ms.
 constexpr int kShadeMinBlocks = ER_SHADE_MIN_BLOCKS;
+constexpr int kShadeGradMinBlocks = ER_SHADE_GRAD_MIN_BLOCKS;
 
 template <bool BATCH, bool GRAD = false>
-__global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
+__global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlocks)
     k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B, GradArgs G) {
   const int32_t qin = bounce & 1;
   const int32_t n = w.counts[kExt + qin];
@@ -363,7 +356,7 @@ __global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
       float4 L = w.light[p];
       const uint32_t fl_prev = GRAD ? __float_as_uint(w.pend[4 * (size_t)p + 2].w) : 0u;
       resolve(w, p, L);
-      if (GRAD && (fl_prev & 1u)) grad_prev_vertex(S, P, w, G, p, local, fl_prev, L);
+      if (GRAD && (fl_prev & 1u)) grad_prev_vertex(w, G, p, fl_prev);
       float4 T4 = w.thr[p];
       f3 thr = mk(T4.x, T4.y, T4.z);
       float4 h = w.hits[i];
@@ -387,9 +380,9 @@ __global__ void __launch_bounds__(128, GRAD ? 1 : kShadeMinBlocks)
         VertexShade V;
         shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
         if (GRAD) {
-          w.g_vo[p] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
-          w.g_vd[p] = make_float4(d.x, d.y, d.z, __int_as_float(bounce));
-          w.g_vh[p] = make_float4(h.x, h.y, h.z, 0.f);
+          const float4 dl4 = w.g_dl[p], lt = w.g_lt[p];
+          vertex_grad_coeffs(S, V, thr, mk(dl4.x, dl4.y, dl4.z), mk(lt.x, lt.y, lt.z), mk(L.x, L.y, L.z),
+                             w.g_k + 5 * (size_t)p);
         }
         env_o = V.env_o;
         env_d = V.env_d;
@@ -461,7 +454,7 @@ __global__ void k_resolve_grad(DevScene S, WaveView w, WaveParams P, int32_t n, 
   if (!(fl & 1u)) return;
   float4 L = w.light[p];
   resolve(w, p, L);
-  grad_prev_vertex(S, P, w, G, p, p, fl, L);
+  grad_prev_vertex(w, G, p, fl);
 }
 
 // kernel.cu:445-478 per pixel, samples in index order.
@@ -615,9 +608,7 @@ er_status wave_fill(Wave* ww, int64_t cap, bool aov, bool grad, unsigned long lo
   if (grad) {
     AL(w->g_lt, cap * sizeof(float4));
     AL(w->g_dl, cap * sizeof(float4));
-    AL(w->g_vo, cap * sizeof(float4));
-    AL(w->g_vd, cap * sizeof(float4));
-    AL(w->g_vh, cap * sizeof(float4));
+    AL(w->g_k, 5 * cap * sizeof(float4));
   }
 #undef AL
   return ER_OK;
