@@ -14,19 +14,26 @@
 //     HPG 2012), duplicate codes ordered by index;
 //  4. bottom-up bounds, triangle counts and shading-offset maxima, the last
 //     child to finish computing its parent;
+//  4b. treelet restructuring (T. Karras and T. Aila, "Fast parallel
+//     construction of high-quality bounding volume hierarchies", HPG 2013):
+//     bottom-up again, each node grows a treelet of up to 7 leaves (opening
+//     the largest-area internal leaf) and rebuilds it with the topology of
+//     least SAH cost, found by dynamic programming over the leaf subsets;
+//     three passes; then the triangles are renumbered into the tree's leaf
+//     order so that every subtree is again a contiguous range;
 //  5. top-down collapse, one launch per level: a binary node with more than
 //     max_leaf triangles becomes a 4-wide node whose children are found by
 //     repeatedly opening the largest-area internal child; a subtree with at
 //     most max_leaf triangles becomes a leaf reference over its contiguous
 //     range of sorted triangles;
 //  6. the triangle arrays are gathered into leaf (sorted) order.
-// Trees built this way trace slower than the host SAH tree; building is
-// ~100x faster.
+// Without step 4b such trees trace ~12 % slower than the host SAH tree.
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -41,6 +48,7 @@ struct BNode {            // binary radix-tree node
   int32_t first, last;    // sorted triangle range
   int32_t parent;
   int32_t count;
+  float cost;             // SAH cost of the subtree (step 4b)
 };
 
 __device__ __forceinline__ uint64_t spread21(uint32_t v) {
@@ -173,16 +181,237 @@ __global__ void k_bottom_up(const float* pos, const int32_t* sorted, const float
   }
 }
 
-struct Item {
-  int32_t bnode;   // binary node to expand into a 4-wide node
-  int32_t out;     // its 4-wide node index
-};
-
 __device__ __forceinline__ float area_of(const float* lo, const float* hi) {
   float x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
   if (!(x >= 0.f) || !(y >= 0.f) || !(z >= 0.f)) return 0.f;
   return 2.f * (x * y + x * z + y * z);
 }
+
+// ------------------------------------------------------- treelets (4b) --
+
+constexpr float kSahNode = 1.2f, kSahTri = 1.0f;  // as the host builder's SAH
+constexpr int kTreelet = 7;                         // leaves per treelet
+
+__device__ __forceinline__ void tri_box(const float* pos, const int32_t* sorted, int32_t leaf, float* lo, float* hi) {
+  const float* p = pos + 9 * (int64_t)sorted[leaf];
+  for (int k = 0; k < 3; k++) {
+    lo[k] = fminf(fminf(p[k], p[3 + k]), p[6 + k]);
+    hi[k] = fmaxf(fmaxf(p[k], p[3 + k]), p[6 + k]);
+  }
+}
+
+// Bounds, count, delta and cost of a node or leaf as other threads left
+// them (read through L2).
+struct Sub {
+  float lo[3], hi[3], delta, cost;
+  int32_t count;
+};
+__device__ __forceinline__ Sub sub_of(const BNode* nodes, const float* pos, const int32_t* sorted, const float* tdelta,
+                                      int32_t c) {
+  Sub r;
+  if (c < 0) {
+    tri_box(pos, sorted, ~c, r.lo, r.hi);
+    r.delta = tdelta[sorted[~c]];
+    r.count = 1;
+    r.cost = kSahTri * area_of(r.lo, r.hi);
+  } else {
+    const BNode* b = nodes + c;
+    for (int k = 0; k < 3; k++) {
+      r.lo[k] = __ldcg(&b->lo[k]);
+      r.hi[k] = __ldcg(&b->hi[k]);
+    }
+    r.delta = __ldcg(&b->delta);
+    r.count = __ldcg(&b->count);
+    r.cost = __ldcg(&b->cost);
+  }
+  return r;
+}
+
+// Sets node nd from its two children (bounds, count, delta, cost).
+__device__ __forceinline__ void refit(BNode* nodes, const float* pos, const int32_t* sorted, const float* tdelta,
+                                      int32_t nd) {
+  BNode& b = nodes[nd];
+  const Sub l = sub_of(nodes, pos, sorted, tdelta, __ldcg(&b.left));
+  const Sub r = sub_of(nodes, pos, sorted, tdelta, __ldcg(&b.right));
+  for (int k = 0; k < 3; k++) {
+    b.lo[k] = fminf(l.lo[k], r.lo[k]);
+    b.hi[k] = fmaxf(l.hi[k], r.hi[k]);
+  }
+  b.delta = fmaxf(l.delta, r.delta);
+  b.count = l.count + r.count;
+  b.cost = kSahNode * area_of(b.lo, b.hi) + l.cost + r.cost;
+}
+
+// Bottom-up: the second child to arrive restructures the treelet rooted at
+// its parent.  Everything below the root is final by then, and no other
+// thread touches it again; the root keeps its place (and parent).
+__global__ void k_treelets(const float* pos, const int32_t* sorted, const float* tdelta, int32_t n, BNode* nodes,
+                           int32_t* leaf_parent, int32_t* visits, int32_t* err) {
+  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int32_t cur = leaf_parent[k];
+  for (int32_t steps = 0; cur >= 0; steps++) {
+    if (steps >= n || cur >= n - 1) {  // a walk longer than the tree: corrupt links
+      atomicOr(err, 1);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(&visits[cur], 1) == 0) return;
+    __threadfence();
+    BNode* R = nodes + cur;
+    // grow the treelet
+    int32_t T[kTreelet], I[kTreelet - 1];
+    int nt = 2, ni = 1;
+    T[0] = __ldcg(&R->left);
+    T[1] = __ldcg(&R->right);
+    I[0] = cur;
+    while (nt < kTreelet) {
+      int pick = -1;
+      float pa = -1.f;
+      for (int j = 0; j < nt; j++) {
+        if (T[j] < 0) continue;
+        const Sub sj = sub_of(nodes, pos, sorted, tdelta, T[j]);
+        const float a = area_of(sj.lo, sj.hi);
+        if (a > pa) { pa = a; pick = j; }
+      }
+      if (pick < 0) break;
+      const int32_t t = T[pick];
+      I[ni++] = t;
+      T[pick] = __ldcg(&nodes[t].left);
+      T[nt++] = __ldcg(&nodes[t].right);
+    }
+    if (nt >= 3) {
+      // least-cost topology over the treelet's leaves
+      float tlo[kTreelet][3], thi[kTreelet][3], tc[kTreelet];
+      for (int j = 0; j < nt; j++) {
+        const Sub sj = sub_of(nodes, pos, sorted, tdelta, T[j]);
+        for (int a = 0; a < 3; a++) { tlo[j][a] = sj.lo[a]; thi[j][a] = sj.hi[a]; }
+        tc[j] = sj.cost;
+      }
+      float cost[1 << kTreelet];
+      uint8_t part[1 << kTreelet];
+      const int full = (1 << nt) - 1;
+      for (int sset = 1; sset <= full; sset++) {
+        if ((sset & (sset - 1)) == 0) {
+          cost[sset] = tc[__ffs(sset) - 1];
+          continue;
+        }
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int j = 0; j < nt; j++)
+          if (sset >> j & 1)
+            for (int a = 0; a < 3; a++) { lo[a] = fminf(lo[a], tlo[j][a]); hi[a] = fmaxf(hi[a], thi[j][a]); }
+        const int low = sset & -sset, rest = sset ^ low;
+        float best = INFINITY;
+        int bp = low;
+        // partitions {low | q, rest \ q}, q a proper subset of rest
+        for (int q = (rest - 1) & rest;; q = (q - 1) & rest) {
+          const int pp = low | q;
+          const float c = cost[pp] + cost[sset ^ pp];
+          if (c < best) { best = c; bp = pp; }
+          if (q == 0) break;
+        }
+        cost[sset] = kSahNode * area_of(lo, hi) + best;
+        part[sset] = (uint8_t)bp;
+      }
+      // current cost of the treelet
+      const Sub l0 = sub_of(nodes, pos, sorted, tdelta, __ldcg(&R->left));
+      const Sub r0 = sub_of(nodes, pos, sorted, tdelta, __ldcg(&R->right));
+      float rlo[3], rhi[3];
+      for (int a = 0; a < 3; a++) { rlo[a] = fminf(l0.lo[a], r0.lo[a]); rhi[a] = fmaxf(l0.hi[a], r0.hi[a]); }
+      const float now = kSahNode * area_of(rlo, rhi) + l0.cost + r0.cost;
+      if (cost[full] < now * (1.0f - 1e-6f)) {
+        // rebuild with the internal nodes I (I[0] = the root), parents first
+        int32_t st_s[kTreelet], st_n[kTreelet];
+        int sp = 0, used = 1;
+        int32_t order[kTreelet - 1];
+        int no = 0;
+        st_s[sp] = full;
+        st_n[sp++] = cur;
+        while (sp > 0) {
+          const int sset = st_s[--sp];
+          const int32_t nd = st_n[sp];
+          order[no++] = nd;
+          const int sides[2] = {part[sset], sset ^ part[sset]};
+          int32_t ch[2];
+          for (int c = 0; c < 2; c++) {
+            if ((sides[c] & (sides[c] - 1)) == 0) {
+              ch[c] = T[__ffs(sides[c]) - 1];
+            } else {
+              ch[c] = I[used++];
+              st_s[sp] = sides[c];
+              st_n[sp++] = ch[c];
+            }
+            if (ch[c] >= 0) nodes[ch[c]].parent = nd;
+            else leaf_parent[~ch[c]] = nd;
+          }
+          nodes[nd].left = ch[0];
+          nodes[nd].right = ch[1];
+        }
+        // children before parents
+        for (int o = no - 1; o >= 0; o--) refit(nodes, pos, sorted, tdelta, order[o]);
+      } else {
+        R->cost = now;
+      }
+    } else {
+      refit(nodes, pos, sorted, tdelta, cur);
+    }
+    cur = __ldcg(&R->parent);
+  }
+}
+
+// Position of leaf k in the tree's left-to-right leaf order.
+__global__ void k_leaf_order(const BNode* nodes, const int32_t* leaf_parent, int32_t n, int32_t* pos_of, int32_t* err) {
+  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int32_t child = ~k, nd = leaf_parent[k], p = 0;
+  for (int32_t steps = 0; nd >= 0; steps++) {
+    if (steps >= n || nd >= n - 1) {
+      atomicOr(err, 2);
+      pos_of[k] = k;
+      return;
+    }
+    const BNode& b = nodes[nd];
+    if (b.right == child) p += b.left < 0 ? 1 : nodes[b.left].count;
+    child = nd;
+    nd = b.parent;
+  }
+  pos_of[k] = p;
+}
+
+// Renumbers leaves to their positions: triangle order, leaf references,
+// first / last of every internal node.
+__global__ void k_renumber_leaves(const int32_t* sorted, const int32_t* pos_of, int32_t n, int32_t* sorted2) {
+  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) sorted2[pos_of[k]] = sorted[k];
+}
+__global__ void k_renumber_nodes(BNode* nodes, const int32_t* pos_of, int32_t n_int) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_int) return;
+  BNode& b = nodes[i];
+  if (b.left < 0) b.left = ~pos_of[~b.left];
+  if (b.right < 0) b.right = ~pos_of[~b.right];
+}
+__global__ void k_node_ranges(BNode* nodes, const int32_t* pos_of, int32_t n_int, int32_t* err) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_int) return;
+  // leftmost leaf (references already renumbered by the previous launch)
+  int32_t c = i;
+  for (int32_t steps = 0; c >= 0; steps++) {
+    if (steps > n_int || c >= n_int) {
+      atomicOr(err, 4);
+      return;
+    }
+    c = nodes[c].left;
+  }
+  nodes[i].first = ~c;
+  nodes[i].last = ~c + nodes[i].count - 1;
+}
+
+struct Item {
+  int32_t bnode;   // binary node to expand into a 4-wide node
+  int32_t out;     // its 4-wide node index
+};
+
 
 // Child c (>= 0 internal, < 0 ~leaf) bounds / count / delta / range
 __device__ __forceinline__ void child_info(const BNode* nodes, const float* pos, const int32_t* sorted,
@@ -378,6 +607,29 @@ er_status build_bvh_gpu(er_scene* s, const er_scene_desc* d, int max_leaf, const
     k_bottom_up<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pos, sorted, tdelta, n, bn, leaf_parent, visits);
   }
   ER_CUDA(cudaGetLastError());
+  if (n > 2) {
+    // treelet restructuring, then triangles renumbered into leaf order
+    int32_t *pos_of, *sorted2, *terr;
+    if ((e = X.get((void**)&pos_of, (size_t)n * 4)) != ER_OK) return e;
+    if ((e = X.get((void**)&sorted2, (size_t)n * 4)) != ER_OK) return e;
+    if ((e = X.get((void**)&terr, 4)) != ER_OK) return e;
+    ER_CUDA(cudaMemsetAsync(terr, 0, 4, st));
+    for (int pass = 0; pass < 3; pass++) {
+      ER_CUDA(cudaMemsetAsync(visits, 0, (size_t)(n - 1) * 4, st));
+      k_treelets<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(pos, sorted, tdelta, n, bn, leaf_parent, visits, terr);
+    }
+    const unsigned gb = (unsigned)((n + 255) / 256);
+    k_leaf_order<<<gb, 256, 0, st>>>(bn, leaf_parent, n, pos_of, terr);
+    k_renumber_leaves<<<gb, 256, 0, st>>>(sorted, pos_of, n, sorted2);
+    k_renumber_nodes<<<gb, 256, 0, st>>>(bn, pos_of, n - 1);
+    k_node_ranges<<<gb, 256, 0, st>>>(bn, pos_of, n - 1, terr);
+    ER_CUDA(cudaGetLastError());
+    int32_t herr = 0;
+    ER_CUDA(cudaMemcpyAsync(&herr, terr, 4, cudaMemcpyDeviceToHost, st));
+    ER_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(ER_ERR_DEVICE_CHECK, "GPU BVH treelet pass: corrupt tree links (" + std::to_string(herr) + ")");
+    sorted = sorted2;
+  }
 
   // top-down collapse into 4-wide nodes, one launch per level
   float* nodes4;
