@@ -133,6 +133,24 @@ __device__ __forceinline__ f3 sample_adjoint(f3 L, float4 g4, uint32_t n) {
             (keep && L.z > 0.f && L.z < 10.f) ? g4.z * inv_n : 0.f);
 }
 
+// Path order within a sample: 8x4 pixel tiles (a warp's 32 paths start in
+// one tile, so its primary rays and first hits are coherent) when the image
+// divides into them, else raster order.  pix = y * W + x either way; the
+// random numbers and the output slot depend only on the pixel, so the order
+// changes no result.
+__device__ __forceinline__ bool tiled(const WaveParams& P) { return (P.W & 7) == 0 && (P.H & 3) == 0; }
+__device__ __forceinline__ int32_t path_pixel(const WaveParams& P, int32_t q) {
+  if (!tiled(P)) return q;
+  const int32_t t = q >> 5, r = q & 31, tw = P.W >> 3;
+  const int32_t x = ((t % tw) << 3) + (r & 7), y = ((t / tw) << 2) + (r >> 3);
+  return y * P.W + x;
+}
+__device__ __forceinline__ int32_t pixel_path(const WaveParams& P, int32_t pix) {
+  if (!tiled(P)) return pix;
+  const int32_t x = pix % P.W, y = pix / P.W;
+  return (((y >> 2) * (P.W >> 3) + (x >> 3)) << 5) + ((y & 3) << 3) + (x & 7);
+}
+
 template <bool BATCH, bool GRAD = false>
 __global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchView B, GradArgs G) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,7 +161,7 @@ __global__ void k_raygen(DevScene S, WaveView w, WaveParams P, int32_t n, BatchV
   if (p >= n) return;
   int32_t job;
   int32_t local = path_slice<BATCH>(B, p, P, job);
-  int32_t pix = local % P.npix, s = local / P.npix;
+  int32_t pix = path_pixel(P, local % P.npix), s = local / P.npix;
   int32_t x = pix % P.W, y = pix / P.W;
   uint32_t idx = (uint32_t)out_index(P, x, y);
   uint32_t sample = (uint32_t)(P.sample_base + s);
@@ -375,7 +393,7 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
         L.z = __fadd_rn(L.z, __fmul_rn(e.z, thr.z));
         w.bounces[p] = bounce;
       } else {
-        int32_t pix = local % P.npix, s = local / P.npix;
+        int32_t pix = path_pixel(P, local % P.npix), s = local / P.npix;
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         VertexShade V;
         shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
@@ -492,7 +510,7 @@ __device__ __forceinline__ void accumulate_pixel(const WaveView& w, const WavePa
   float4 a[3];
   if (F.aov_on) for (int k = 0; k < 3; k++) a[k] = F.aov[k][idx];
   for (int32_t s = 0; s < sw; s++) {
-    int32_t p = path_base + s * P.npix + pix;
+    int32_t p = path_base + s * P.npix + pixel_path(P, pix);
     float4 L = w.light[p];
     resolve(w, p, L);
     if (F.keep) {
@@ -546,7 +564,7 @@ __global__ void k_dump(WaveView w, WaveParams P, int32_t sw, int32_t s_off, floa
   if (p >= sw * P.npix) return;
   float4 L = w.light[p];
   resolve(w, p, L);
-  int32_t pix = p % P.npix, s = p / P.npix;
+  int32_t pix = path_pixel(P, p % P.npix), s = p / P.npix;
   int64_t j = (int64_t)(s + s_off) * P.npix + out_index(P, pix % P.W, pix / P.W);
   rad[3 * j] = L.x; rad[3 * j + 1] = L.y; rad[3 * j + 2] = L.z;
   bnc[j] = w.bounces[p];
