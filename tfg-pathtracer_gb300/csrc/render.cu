@@ -649,15 +649,15 @@ er_status ensure_wave(er_scene* s, int64_t cap, bool aov, bool grad = false) {
 
 // The second wave of the two-stream schedule, its stream and events; the
 // same capacity and passes as the first.
-er_status ensure_wave2(er_scene* s) {
+er_status ensure_wave2(er_scene* s, bool grad = false) {
   const Wave* w1 = s->wave;
-  if (!s->wave2 || s->wave2->cap < w1->cap || (w1->v.aov && !s->wave2->v.aov)) {
+  if (!s->wave2 || s->wave2->cap < w1->cap || (w1->v.aov && !s->wave2->v.aov) || (grad && !s->wave2->v.g_lt)) {
     if (s->wave2) {
       for (void* p : s->wave2->mem) cudaFree(p);
       delete s->wave2;
     }
     s->wave2 = new Wave();
-    er_status st = wave_fill(s->wave2, w1->cap, w1->v.aov, false, s->d_stats);
+    er_status st = wave_fill(s->wave2, w1->cap, w1->v.aov, grad || w1->v.g_lt, s->d_stats);
     if (st != ER_OK) {
       for (void* p : s->wave2->mem) cudaFree(p);
       delete s->wave2;
@@ -902,7 +902,14 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
   sw = std::min(sw, std::max(1, o->spp));
   er_status st = ensure_wave(s, (int64_t)sw * npix, false, true);
   if (st != ER_OK) return st;
-  WaveView& w = s->wave->v;
+  // waves alternate between two pipelines as in run(); the gradients are
+  // atomic sums, so the waves need no order between them
+  const bool two = o->spp > sw;
+  if (two) {
+    if ((st = ensure_wave2(s, true)) != ER_OK) return st;
+    ER_CUDA(cudaEventRecord(s->ev_fork, s->stream));
+    ER_CUDA(cudaStreamWaitEvent(s->stream2, s->ev_fork, 0));
+  }
   WaveParams P;
   P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
   P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
@@ -914,22 +921,30 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
     g_sh = grid_for(k_shade<false, true>, 128, s->num_sms);
   }
   const BatchView NB;
-  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+  int32_t k = 0;
+  for (int32_t s0 = 0; s0 < o->spp; s0 += sw, k++) {
+    const bool alt = two && (k & 1);
+    WaveView& w = alt ? s->wave2->v : s->wave->v;
+    cudaStream_t strm = alt ? s->stream2 : s->stream;
     const int32_t cur = std::min(sw, o->spp - s0);
     P.spp_wave = cur;
     P.sample_base = o->sample_begin + s0;
     const int32_t n = cur * npix;
-    k_raygen<false, true><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, G);
+    k_raygen<false, true><<<(n + 255) / 256, 256, 0, strm>>>(s->dev, w, P, n, NB, G);
     for (int32_t b = 0; b <= max_depth; b++) {
       if (s->dev.use_q8)
-        k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+        k_trace<true, false, false><<<g_tr[1], kTravBlock, 0, strm>>>(s->dev, w, b, s->err_word, NB, 7u);
       else
-        k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+        k_trace<false, false, false><<<g_tr[0], kTravBlock, 0, strm>>>(s->dev, w, b, s->err_word, NB, 7u);
       if (b == max_depth) break;
-      k_shade<false, true><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB, G);
+      k_shade<false, true><<<g_sh, 128, 0, strm>>>(s->dev, w, P, b, NB, G);
     }
-    k_resolve_grad<<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, G);
+    k_resolve_grad<<<(n + 255) / 256, 256, 0, strm>>>(s->dev, w, P, n, G);
     ER_CUDA(cudaGetLastError());
+  }
+  if (two) {
+    ER_CUDA(cudaEventRecord(s->ev_acc[0], s->stream2));
+    ER_CUDA(cudaStreamWaitEvent(s->stream, s->ev_acc[0], 0));
   }
   return ER_OK;
 }
