@@ -93,6 +93,35 @@ def test_q8_bvh_same_hits(c0):
     q8.close()
 
 
+@pytest.mark.parametrize("scale", [1.0, 1e11])
+def test_q8_bvh_same_hits_axis_rays_and_huge_extents(c0, scale):
+    """Rays along the axes (direction components 0: reciprocal 2^100) on the
+    scene as given and scaled to an extent of ~1e12, where the Q8 decode's
+    scale * reciprocal overflows and the node falls back to the plain
+    decode: FP32 and Q8 nodes give the same hits."""
+    import dataclasses
+    arrays, _, _ = c0
+    big = dataclasses.replace(arrays, positions=(arrays.positions.astype(np.float64) * scale).astype(np.float32))
+    fp = _lib.Scene(big)
+    q8 = _lib.Scene(big, bvh_format=A.ER_BVH_Q8)
+    rng = np.random.default_rng(7)
+    lo = big.positions.reshape(-1, 3).min(0)
+    hi = big.positions.reshape(-1, 3).max(0)
+    n = 60_000
+    o = (lo + (hi - lo) * rng.random((n, 3))).astype(np.float32)
+    d = np.zeros((n, 3), np.float32)
+    axis = rng.integers(0, 3, n)
+    d[np.arange(n), axis] = np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    rays = np.concatenate([o, d], 1)
+    t1, d1, _, _ = fp.trace(rays)
+    t2, d2, _, _ = q8.trace(rays)
+    assert (t1 >= 0).sum() > 1000
+    assert np.array_equal(t1, t2)
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+    fp.close()
+    q8.close()
+
+
 def test_render_paths_match_oracle(c0):
     arrays, scene, orc = c0
     rad, b = scene.render_paths(spp=2, max_depth=4, seed=11)
