@@ -103,10 +103,11 @@ def test_search_lookup_table_matches_the_oracle_per_path():
     orc = O.OrcScene(arrays)
     rad, b = scene.render_paths(spp=2, max_depth=4, seed=13)
     rrad, rb = orc.render_paths(spp=2, max_depth=4, seed=13)
-    assert (b == rb).mean() > 0.99
+    # measured: bounce counts 100 %, radiance 99.97 % (98.5 % bit for bit)
+    assert (b == rb).mean() > 0.999
     close = np.isclose(rad, rrad, rtol=1e-3, atol=1e-5).all(axis=2)
     both_nan = np.isnan(rad).any(2) & np.isnan(rrad).any(2)
-    assert (close | both_nan).mean() > 0.98
+    assert (close | both_nan).mean() > 0.999
     a = scene.render(4, max_depth=4, seed=2)["beauty"]
     other = _lib.Scene(arrays)
     c = other.render(4, max_depth=4, seed=2)["beauty"]

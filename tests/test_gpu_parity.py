@@ -130,8 +130,9 @@ def test_render_paths_match_oracle(c0):
     close = np.isclose(rad, rrad, rtol=1e-3, atol=1e-5).all(axis=2)
     both_nan = np.isnan(rad).any(2) & np.isnan(rrad).any(2)
     frac = (close | both_nan).mean()
-    assert same_b > 0.99, f"bounce counts agree on {same_b:.4f} of paths"
-    assert frac > 0.98, f"per-path radiance agrees on {frac:.4f} of paths"
+    # measured: bounce counts 100 %, radiance 99.99 % (85 % bit for bit)
+    assert same_b > 0.999, f"bounce counts agree on {same_b:.4f} of paths"
+    assert frac > 0.999, f"per-path radiance agrees on {frac:.4f} of paths"
 
 
 def test_render_image_matches_oracle(c0):
