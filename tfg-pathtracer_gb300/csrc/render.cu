@@ -465,13 +465,12 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
 
 // Gradient of every path's last shaded vertex (resolved here instead of in
 // the accumulation).
-__global__ void k_resolve_grad(DevScene S, WaveView w, WaveParams P, int32_t n, GradArgs G) {
+__global__ void k_resolve_grad(WaveView w, int32_t n, GradArgs G) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const uint32_t fl = __float_as_uint(w.pend[4 * (size_t)p + 2].w);
   if (!(fl & 1u)) return;
-  float4 L = w.light[p];
-  resolve(w, p, L);
+  w.pend[4 * (size_t)p + 2].w = __uint_as_float(0u);
   grad_prev_vertex(w, G, p, fl);
 }
 
@@ -939,7 +938,7 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
       if (b == max_depth) break;
       k_shade<false, true><<<g_sh, 128, 0, strm>>>(s->dev, w, P, b, NB, G);
     }
-    k_resolve_grad<<<(n + 255) / 256, 256, 0, strm>>>(s->dev, w, P, n, G);
+    k_resolve_grad<<<(n + 255) / 256, 256, 0, strm>>>(w, n, G);
     ER_CUDA(cudaGetLastError());
   }
   if (two) {
