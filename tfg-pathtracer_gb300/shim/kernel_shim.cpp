@@ -129,7 +129,9 @@ cudaError_t renderSetup(Scene* scene) {
 
 // kernel.cu:665-686: sampleTarget more samples per pixel, MAXBOUNCES deep.
 cudaError_t renderCuda(Scene*, int sampleTarget) {
-  const int chunk = 4;
+  // 8 samples per call: two waves in flight at 1080p (a 4-sample call is a
+  // single wave), and the polling thread still sees a new image every ~30 ms
+  const int chunk = 8;
   for (int done = 0; done < sampleTarget; done += chunk) {
     std::lock_guard<std::mutex> lk(g_lock);
     er_render_opts o{};
