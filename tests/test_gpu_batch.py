@@ -43,6 +43,8 @@ def world():
         dict(scene=2, spp=8, max_depth=3, seed=3, camera=cams[2], flags=A.ER_RENDER_ENV_ALIAS),
         dict(scene=1, spp=4, max_depth=5, seed=4, camera=_moved(cams[1], 0.7, (72, 40)), sample_begin=3),
         dict(scene=0, spp=2, max_depth=8, seed=5, camera=_moved(cams[0], -1.0), flags=A.ER_RENDER_ACCUM_FP64),
+        # a resolution without 8x4 path tiles (raster path order)
+        dict(scene=2, spp=3, max_depth=4, seed=6, camera=_moved(cams[2], 0.3, (70, 38))),
     ]
     return arrays, fp32, q8, jobs
 
