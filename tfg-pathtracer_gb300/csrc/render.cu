@@ -631,11 +631,16 @@ er_status wave_fill(Wave* ww, int64_t cap, bool aov, bool grad, unsigned long lo
   return ER_OK;
 }
 
-// Default path budget of a wave (about 2.3 GB of buffers; two waves are in
-// flight): at 1080p four samples per pixel.  Larger waves lose less to the
-// tails of the traversal launches: 8.04 ms per 1080p sample against 8.25 ms
-// at half this budget and 7.95 ms at twice it.
-constexpr int64_t kWavePaths = (int64_t)1 << 23;
+// Default path budget of a wave (about 4.6 GB of buffers; two waves are in
+// flight): at 1080p eight samples per pixel.  Larger waves lose less to the
+// tails of the traversal launches (per 1080p sample: 8.25 ms at 2^22 paths,
+// 8.04 at 2^23, 7.95 at 2^24), but a call keeps at least two waves when it
+// has two samples, so that its waves overlap on two streams.
+constexpr int64_t kWavePaths = (int64_t)1 << 24;
+int32_t default_spp_per_wave(int32_t spp, int32_t npix) {
+  const int32_t budget = std::max(1, (int32_t)(kWavePaths / npix));
+  return std::max(1, std::min(budget, (spp + 1) / 2));
+}
 
 er_status ensure_wave(er_scene* s, int64_t cap, bool aov, bool grad = false) {
   if (s->wave && s->wave->cap >= cap && (!aov || s->wave->v.aov) && (!grad || s->wave->v.g_lt)) return ER_OK;
@@ -721,7 +726,7 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
   const int32_t npix = W * H;
   const bool aov = o->flags & ER_RENDER_AOV;
   int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
-  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : std::max(1, (int32_t)(kWavePaths / npix));
+  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : default_spp_per_wave(o->spp, npix);
   sw = std::min(sw, std::max(1, o->spp));
   er_status st = ensure_wave(s, (int64_t)sw * npix, aov, grad_wave);
   if (st != ER_OK) return st;
@@ -897,7 +902,7 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
   const int32_t W = s->camera.x_res, H = s->camera.y_res;
   const int32_t npix = W * H;
   const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
-  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : std::max(1, (int32_t)(kWavePaths / npix));
+  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : default_spp_per_wave(o->spp, npix);
   sw = std::min(sw, std::max(1, o->spp));
   er_status st = ensure_wave(s, (int64_t)sw * npix, false, true);
   if (st != ER_OK) return st;
