@@ -110,7 +110,9 @@ typedef struct er_scene_desc {
   const float* tangent_sign; /* tri_count, NULL = +1                         */
   const int32_t* tri_object; /* tri_count: mesh object of each triangle     */
   int32_t object_count;
-  const int32_t* object_material; /* object_count: material of each object */
+  const int32_t* object_material; /* object_count: material of each object;
+                                     ignored (material 0) when object_count
+                                     is 0                                    */
   int32_t material_count;
   const er_material* materials;
   int32_t texture_count;

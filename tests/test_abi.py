@@ -98,6 +98,37 @@ def test_invalid_arguments_rejected():
     assert L.er_render(None, None, None, None, None, None, None, None, None) == 1
 
 
+def test_descriptor_checks_before_any_device_call():
+    """NULL arrays with positive counts and non-finite camera fields are
+    rejected as invalid arguments (no device is touched first)."""
+    L = _lib.load()
+    h = C.c_void_p()
+    arr = scenes.config0(8, 6, n_spheres=1, subdiv=0)
+
+    def rejected(edit, word):
+        d, keep = arr.desc()
+        edit(d)
+        assert L.er_scene_create(C.byref(d), None, C.byref(h)) == A.ER_ERR_INVALID_ARG
+        assert word in L.er_last_error(), L.er_last_error()
+        assert not h.value
+
+    rejected(lambda d: setattr(d, "materials", None), b"materials is NULL")
+    def no_textures(d):
+        d.texture_count = 1
+        d.textures = None
+    rejected(no_textures, b"textures is NULL")
+    rejected(lambda d: setattr(d, "lights", None), b"lights is NULL")
+
+    def nan_pose(d):
+        d.camera.position[1] = float("nan")
+    rejected(nan_pose, b"camera pose")
+
+    def inf_focal(d):
+        d.camera.focal_length = float("inf")
+    rejected(inf_focal, b"camera parameter")
+    assert L.er_scene_set_camera(None, None) == A.ER_ERR_INVALID_ARG
+
+
 def test_no_device_is_reported_not_faked():
     """Without a GPU the library reports it; there is no CPU fallback."""
     try:

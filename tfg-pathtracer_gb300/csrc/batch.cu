@@ -519,8 +519,8 @@ extern "C" er_status er_batch_set_jobs(er_batch* b, const er_batch_job* jobs, in
   for (int32_t j = 0; j < n_jobs; j++) {
     const er_batch_job& J = jobs[j];
     if (J.scene < 0 || J.scene >= (int32_t)b->scenes.size()) return fail(ER_ERR_INVALID_ARG, "job scene out of range");
-    if (J.camera.x_res <= 0 || J.camera.y_res <= 0 || (int64_t)J.camera.x_res * J.camera.y_res > ((int64_t)1 << 28))
-      return fail(ER_ERR_INVALID_ARG, "job camera resolution out of range");
+    er_status cs = validate_camera(J.camera);
+    if (cs != ER_OK) return fail(cs, "job " + std::to_string(j) + ": " + er_last_error());
     if (J.spp < 0 || J.sample_begin < 0 || J.max_depth < 0 || J.max_depth > 64)
       return fail(ER_ERR_INVALID_ARG, "job options out of range");
     if (J.flags & ~(uint32_t)(ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64))

@@ -566,7 +566,10 @@ er_status build_bvh_gpu(er_scene* s, const er_scene_desc* d, int max_leaf, const
   if ((e = X.put(&tan, d->tangents, (size_t)(9 * T), st)) != ER_OK) return e;
   if ((e = X.put(&tsign, d->tangent_sign, (size_t)T, st)) != ER_OK) return e;
   if ((e = X.put(&tobj, d->tri_object, (size_t)T, st)) != ER_OK) return e;
-  if ((e = X.put(&omat, d->object_material, (size_t)std::max(d->object_count, 0), st)) != ER_OK) return e;
+  // no objects: every triangle takes material 0, as on the host builder
+  if ((e = X.put(&omat, d->object_count > 0 ? d->object_material : nullptr, (size_t)std::max(d->object_count, 0),
+                 st)) != ER_OK)
+    return e;
   if ((e = X.put(&tie, d->tie_key, (size_t)T, st)) != ER_OK) return e;
   float hb[6] = {scene_lo[0], scene_lo[1], scene_lo[2], scene_hi[0] - scene_lo[0], scene_hi[1] - scene_lo[1],
                  scene_hi[2] - scene_lo[2]};

@@ -40,18 +40,20 @@ double fast_pow(double a, double b) {
   return r;
 }
 
-uint32_t crc32(const uint8_t* p, size_t n, uint32_t c = 0xFFFFFFFFu) {
-  static uint32_t table[256];
-  static bool init = false;
-  if (!init) {
+struct CrcTable {
+  uint32_t v[256];
+  CrcTable() {
     for (uint32_t i = 0; i < 256; i++) {
-      uint32_t v = i;
-      for (int k = 0; k < 8; k++) v = (v & 1) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
-      table[i] = v;
+      uint32_t x = i;
+      for (int k = 0; k < 8; k++) x = (x & 1) ? 0xEDB88320u ^ (x >> 1) : x >> 1;
+      v[i] = x;
     }
-    init = true;
   }
-  for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
+};
+
+uint32_t crc32(const uint8_t* p, size_t n, uint32_t c = 0xFFFFFFFFu) {
+  static const CrcTable table;  // initialised once, thread-safe
+  for (size_t i = 0; i < n; i++) c = table.v[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
   return c;
 }
 

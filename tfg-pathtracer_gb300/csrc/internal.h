@@ -290,6 +290,11 @@ DevCamera make_dev_camera(const er_camera& c);
 void free_wave(er_scene* s);
 void free_film(er_scene* s);
 er_status check_device_error(er_scene* s);
+// Resolution (1 .. 2^28 pixels) and finite lens and pose parameters.
+er_status validate_camera(const er_camera& c);
+// Resident blocks of `block` threads per SM for `kernel` on the current
+// device (at least 1), cached per kernel, block size and device.
+int blocks_per_sm(const void* kernel, int block);
 er_status build_env_alias(er_scene* s);
 // The search lookup table for environments of at least kEnvLutMinTexels
 // texels (no-op below); the tables are refilled after invalidate_env_tables.

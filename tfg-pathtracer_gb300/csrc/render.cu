@@ -12,8 +12,10 @@
 // not depend on queue order.
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include "internal.h"
 #include "shade.cuh"
@@ -579,11 +581,32 @@ __global__ void k_film_clear(Film F, int32_t npix) {
   F.pathcount[i] = 0;
 }
 
+}  // namespace
+
+int blocks_per_sm(const void* kernel, int block) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const auto key = std::make_tuple(kernel, block, dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, block, 0) != cudaSuccess) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  nb = std::max(1, nb);
+  cache[key] = nb;
+  return nb;
+}
+
+namespace {
+
 template <typename K>
 int grid_for(K kernel, int block, int sms) {
-  int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, block, 0);
-  return std::max(1, nb) * sms;
+  return blocks_per_sm((const void*)kernel, block) * sms;
 }
 
 er_status alloc_w(Wave* w, void** p, size_t bytes) {
@@ -746,14 +769,11 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
     ER_CUDA(cudaEventRecord(s->ev_fork, s->stream));
     ER_CUDA(cudaStreamWaitEvent(s->stream2, s->ev_fork, 0));
   }
-  static int g_tr[4] = {0}, g_shade = 0;
-  if (!g_shade) {
-    g_tr[0] = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
-    g_tr[1] = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
-    g_tr[2] = grid_for(k_trace<false, true, false>, kTravBlock, s->num_sms);
-    g_tr[3] = grid_for(k_trace<true, true, false>, kTravBlock, s->num_sms);
-    g_shade = grid_for(k_shade<false>, 128, s->num_sms);
-  }
+  const int g_tr[4] = {grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms),
+                       grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms),
+                       grid_for(k_trace<false, true, false>, kTravBlock, s->num_sms),
+                       grid_for(k_trace<true, true, false>, kTravBlock, s->num_sms)};
+  const int g_shade = grid_for(k_shade<false>, 128, s->num_sms);
   const BatchView NB;
   const int variant = (q8 ? 1 : 0) + (count ? 2 : 0);
   int64_t nl = 0;
@@ -918,12 +938,9 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
   P.W = W; P.H = H; P.npix = npix; P.max_depth = max_depth;
   P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
   P.flags = o->flags & ER_RENDER_ENV_ALIAS;
-  static int g_tr[2] = {0, 0}, g_sh = 0;
-  if (!g_sh) {
-    g_tr[0] = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
-    g_tr[1] = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
-    g_sh = grid_for(k_shade<false, true>, 128, s->num_sms);
-  }
+  const int g_tr[2] = {grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms),
+                       grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms)};
+  const int g_sh = grid_for(k_shade<false, true>, 128, s->num_sms);
   const BatchView NB;
   int32_t k = 0;
   for (int32_t s0 = 0; s0 < o->spp; s0 += sw, k++) {
@@ -985,15 +1002,10 @@ er_status film_clear(const Film& F, cudaStream_t stream) {
 er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, const BatchJobDev* d_jobs,
                        const std::vector<BatchWave>& waves, const BatchSchedule& sch, int num_sms, uint32_t* err,
                        cudaStream_t stream, int64_t* launches, const BatchPair* pair) {
-  static int occ_tr[2] = {0, 0}, occ_sh = 0;  // resident blocks per SM
-  if (!occ_sh) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tr[0], k_trace<false, false, true>, kTravBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tr[1], k_trace<true, false, true>, kTravBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_sh, k_shade<true>, 128, 0);
-    occ_tr[0] = std::max(1, occ_tr[0]);
-    occ_tr[1] = std::max(1, occ_tr[1]);
-    occ_sh = std::max(1, occ_sh);
-  }
+  // resident blocks per SM
+  const int occ_tr[2] = {blocks_per_sm((const void*)k_trace<false, false, true>, kTravBlock),
+                         blocks_per_sm((const void*)k_trace<true, false, true>, kTravBlock)};
+  const int occ_sh = blocks_per_sm((const void*)k_shade<true>, 128);
   const int q8 = S.use_q8 ? 1 : 0;
   const int tb = sch.trace_blocks_per_sm > 0 ? std::min(sch.trace_blocks_per_sm, occ_tr[q8]) : occ_tr[q8];
   const int sb = sch.shade_blocks_per_sm > 0 ? std::min(sch.shade_blocks_per_sm, occ_sh) : occ_sh;
@@ -1325,12 +1337,9 @@ extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, flo
   P.W = W; P.H = H; P.npix = (int32_t)npix; P.max_depth = max_depth;
   P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
   P.flags = 0;
-  static int g_tr = 0, g_tr8 = 0, g_sh = 0;
-  if (!g_sh) {
-    g_tr = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
-    g_tr8 = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
-    g_sh = grid_for(k_shade<false>, 128, s->num_sms);
-  }
+  const int g_tr = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
+  const int g_tr8 = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
+  const int g_sh = grid_for(k_shade<false>, 128, s->num_sms);
   const BatchView NB;
   for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
     int32_t cur = std::min(sw, o->spp - s0);

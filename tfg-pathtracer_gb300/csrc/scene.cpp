@@ -73,6 +73,20 @@ namespace {
 
 bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
+}  // namespace
+
+er_status validate_camera(const er_camera& c) {
+  if (c.x_res <= 0 || c.y_res <= 0 || (int64_t)c.x_res * c.y_res > ((int64_t)1 << 28))
+    return fail(ER_ERR_INVALID_ARG, "camera resolution out of range");
+  float cf[] = {c.focal_length, c.sensor_width, c.sensor_height, c.aperture, c.focus_distance};
+  for (float v : cf)
+    if (!std::isfinite(v)) return fail(ER_ERR_INVALID_ARG, "camera parameter is not finite");
+  if (!finite3(c.position) || !finite3(c.rotation)) return fail(ER_ERR_INVALID_ARG, "camera pose is not finite");
+  return ER_OK;
+}
+
+namespace {
+
 er_status validate_texture(const er_texture& t, const char* what) {
   if (t.width <= 0 || t.height <= 0 || !t.data)
     return fail(ER_ERR_INVALID_ARG, std::string(what) + ": empty texture");
@@ -83,13 +97,8 @@ er_status validate_texture(const er_texture& t, const char* what) {
 
 er_status validate(const er_scene_desc* d) {
   if (!d) return fail(ER_ERR_INVALID_ARG, "desc is NULL");
-  const er_camera& c = d->camera;
-  if (c.x_res <= 0 || c.y_res <= 0 || (int64_t)c.x_res * c.y_res > ((int64_t)1 << 28))
-    return fail(ER_ERR_INVALID_ARG, "camera resolution out of range");
-  float cf[] = {c.focal_length, c.sensor_width, c.sensor_height, c.aperture, c.focus_distance};
-  for (float v : cf)
-    if (!std::isfinite(v)) return fail(ER_ERR_INVALID_ARG, "camera parameter is not finite");
-  if (!finite3(c.position) || !finite3(c.rotation)) return fail(ER_ERR_INVALID_ARG, "camera pose is not finite");
+  er_status cs = validate_camera(d->camera);
+  if (cs != ER_OK) return cs;
   if (d->tri_count < 0 || d->tri_count > kMaxTris - kMaxLeafTris)
     return fail(ER_ERR_INVALID_ARG, "tri_count out of range");
   if (d->tri_count > 0 && !d->positions) return fail(ER_ERR_INVALID_ARG, "positions is NULL");
@@ -104,6 +113,8 @@ er_status validate(const er_scene_desc* d) {
         return fail(ER_ERR_INVALID_ARG, "tri_object index out of range");
   }
   if (d->object_count > 0 && !d->object_material) return fail(ER_ERR_INVALID_ARG, "object_material is NULL");
+  if (d->material_count > 0 && !d->materials) return fail(ER_ERR_INVALID_ARG, "materials is NULL");
+  if (d->texture_count > 0 && !d->textures) return fail(ER_ERR_INVALID_ARG, "textures is NULL");
   for (int32_t i = 0; i < d->object_count; i++)
     if (d->object_material[i] < 0 || d->object_material[i] >= d->material_count)
       return fail(ER_ERR_INVALID_ARG, "object_material index out of range");
@@ -244,7 +255,7 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
     int32_t i = br.order[(size_t)s_];
     const float* p = d->positions + 9 * (int64_t)i;
     int32_t obj = d->tri_object ? d->tri_object[i] : 0;
-    int32_t mat = d->object_material ? d->object_material[obj] : 0;
+    int32_t mat = d->object_material && d->object_count > 0 ? d->object_material[obj] : 0;
     uint32_t key = d->tie_key ? d->tie_key[i] : (uint32_t)i;
     float w[3];
     std::memcpy(&w[0], &i, 4);
@@ -402,8 +413,8 @@ extern "C" er_status er_scene_info_get(const er_scene* s, er_scene_info* out) {
 
 extern "C" er_status er_scene_set_camera(er_scene* s, const er_camera* c) {
   if (!s || !c) return fail(ER_ERR_INVALID_ARG, "NULL argument");
-  if (c->x_res <= 0 || c->y_res <= 0 || (int64_t)c->x_res * c->y_res > ((int64_t)1 << 28))
-    return fail(ER_ERR_INVALID_ARG, "camera resolution out of range");
+  er_status st = validate_camera(*c);
+  if (st != ER_OK) return st;
   s->camera = *c;
   s->dev.cam = make_dev_camera(*c);
   s->version++;
@@ -419,7 +430,11 @@ extern "C" er_status er_scene_get_camera(const er_scene* s, er_camera* out) {
 extern "C" er_status er_scene_free(er_scene* s) {
   if (!s) return ER_OK;
   cudaSetDevice(s->device);
+  // a call that failed part-way may have left work on the second wave's
+  // stream or the snapshot reader: nothing is freed under it
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->stream2) cudaStreamSynchronize(s->stream2);
+  if (s->snap_stream) cudaStreamSynchronize(s->snap_stream);
   free_wave(s);
   free_film(s);
   cudaFree(s->bw_rad);

@@ -38,12 +38,7 @@ __global__ void __launch_bounds__(kTravBlock, kTravMinBlocks)
 
 template <bool Q8, bool STATS>
 void launch(er_scene* s, const float* rays, int64_t n, int normalize, int32_t* tri, float* dist, float* uv) {
-  static int grid = 0;
-  if (!grid) {
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_rays<Q8, STATS>, kTravBlock, 0);
-    grid = (nb > 0 ? nb : 1) * s->num_sms;
-  }
+  const int grid = blocks_per_sm((const void*)k_trace_rays<Q8, STATS>, kTravBlock) * s->num_sms;
   int64_t need = (n + kTravBlock - 1) / kTravBlock;
   int g = (int)(need < grid ? need : grid);
   if (g < 1) g = 1;
