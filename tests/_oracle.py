@@ -8,7 +8,9 @@ import numpy as np
 from eleven import _abi as A
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-ORC_PATH = os.path.join(ROOT, "oracle", "liborc.so")
+# ORC_LIB selects another build of the same sources (oracle/liborc_ulp.so,
+# the rounding-sensitivity probe) for a whole process
+ORC_PATH = os.environ.get("ORC_LIB") or os.path.join(ROOT, "oracle", "liborc.so")
 REF_PATH = os.path.join(ROOT, "oracle", "_ref", "libref.so")
 
 _orc = None
