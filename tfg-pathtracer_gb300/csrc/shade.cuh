@@ -59,9 +59,9 @@ __device__ __forceinline__ int32_t hdri_search(const float* __restrict__ arr, fl
 }
 
 // HDRI.hpp:145-152 (theta from the texel's top edge)
-__device__ __forceinline__ float hdri_pdf(const DevScene& S, int32_t x, int32_t y) {
+// dv: the environment value at storage coordinates (x, y) (tex_coord).
+__device__ __forceinline__ float hdri_pdf(const DevScene& S, f3 dv, int32_t y) {
   const DevTex& t = S.env;
-  f3 dv = tex_coord(S, t, x, y);
   float theta = __fdiv_rn((float)y, (float)t.h) * ER_PI;
   float a = __fdiv_rn((dv.x + dv.y) + dv.z, S.radiance_sum) * (float)t.w * (float)t.h;
   return a / (2.0f * ER_PI * sinf(theta));

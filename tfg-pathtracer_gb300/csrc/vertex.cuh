@@ -29,6 +29,35 @@ __device__ __forceinline__ f3 escape_radiance(const DevScene& S, f3 d, int64_t* 
   return tex_uv(S, E, eu, ev);
 }
 
+// kernel.cu:234-235: index of the environment texel HDRI NEE samples with
+// the shared light uniform r1 = u01(w): the reference's CDF search, or the
+// same search through its 2^24-entry table, or (ER_RENDER_ENV_ALIAS) the
+// alias table of its effective distribution (env.cu).
+__device__ __forceinline__ int32_t env_pick(const DevScene& S, uint32_t flags, uint32_t idx, uint32_t sample,
+                                            int32_t bounce, uint32_t w, uint32_t k0, uint32_t k1) {
+  const DevTex& E = S.env;
+  if ((flags & ER_RENDER_ENV_ALIAS) && S.alias_idx) {
+    // column from the shared light word, coin from a second word
+    uint32_t coin = philox(make_uint4(idx, sample, 2u + (uint32_t)bounce, 1u), k0, k1).x;
+    int32_t col = (int32_t)__umulhi(w, (uint32_t)(E.w * E.h));
+    return coin < __ldg(S.alias_thresh + col) ? col : __ldg(S.alias_idx + col);
+  }
+  if (S.env_lut) return __ldg(S.env_lut + (w >> 8));  // == hdri_search(S.cdf, u01(w), w*h)
+  return hdri_search(S.cdf, u01(w), E.w * E.h);
+}
+
+// kernel.cu:236-245: texel index -> pixel -> uv with the env's tile and
+// offset (Texture.hpp:177-193), limited to [0, 1] (Math.hpp:38-41).
+__device__ __forceinline__ void env_texel_uv(const DevTex& E, int32_t cnt, float& iu, float& iv) {
+  float nu = __fdiv_rn((float)(cnt % E.w), (float)E.w), nv = __fdiv_rn((float)(cnt / E.w), (float)E.h);
+  int32_t ix = __float2int_rz(nu * (float)E.w), iy = __float2int_rz(nv * (float)E.h);
+  ix = __float2int_rz(E.x_tile * ((float)ix - E.x_offset * (float)E.w)) % E.w;
+  iy = __float2int_rz(E.y_tile * ((float)iy - E.y_offset * (float)E.h)) % E.h;
+  iu = __fdiv_rn((float)ix, (float)E.w);
+  iv = __fdiv_rn((float)iy, (float)E.h);
+  limit_uv(iu, iv);
+}
+
 struct VertexShade {
   f3 pos;            // shading position (Tri.hpp:91)
   f3 sn, tg, bt;     // interpolated normal, tangent, bitangent (AOVs)
@@ -61,10 +90,21 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   const float4* tn = S.tri_n + 3 * (size_t)slot;
   float4 v0 = __ldg(tv), v1 = __ldg(tv + 1), v2 = __ldg(tv + 2);
   float4 n0 = __ldg(tn), n1 = __ldg(tn + 1), n2 = __ldg(tn + 2);
+  // The vertex's random numbers and the environment texel they pick for
+  // HDRI NEE (kernel.cu:234-245) depend on no surface data: their loads
+  // (search table, then texel) are issued here, so that they overlap the
+  // triangle -> material -> texture loads below instead of following them.
+  uint4 rn = philox(make_uint4(idx, sample, 2u + (uint32_t)bounce, 0u), k0, k1);
+  const int32_t cnt = env_pick(S, flags, idx, sample, bounce, rn.w, k0, k1);
   f3 sn;
   f3 pos = ref_position(o, d, t, u, v, from4(v0), from4(v1), from4(v2), from4(n0), from4(n1), from4(n2), &sn);
   const float2* tuv = S.tri_uv + 3 * (size_t)slot;
   float2 uv0 = __ldg(tuv), uv1 = __ldg(tuv + 1), uv2 = __ldg(tuv + 2);
+  float iu, iv;
+  env_texel_uv(S.env, cnt, iu, iv);
+  const DevTex& E = S.env;
+  const int32_t ex = __float2int_rz(iu * (float)E.w), ey = __float2int_rz(iv * (float)E.h);
+  const f3 eH = tex_coord(S, E, ex, ey);
   float tu = __fadd_rn(__fadd_rn(uv0.x, __fmul_rn(__fsub_rn(uv1.x, uv0.x), u)), __fmul_rn(__fsub_rn(uv2.x, uv0.x), v));
   float tvv = __fadd_rn(__fadd_rn(uv0.y, __fmul_rn(__fsub_rn(uv1.y, uv0.y), u)), __fmul_rn(__fsub_rn(uv2.y, uv0.y), v));
   f3 tg = mk1(0.f), bt = mk1(0.f);
@@ -108,7 +148,6 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   hd.subsurface = M.subsurface;
   hd.sheen = M.sheen;
 
-  uint4 rn = philox(make_uint4(idx, sample, 2u + (uint32_t)bounce, 0u), k0, k1);
   V.C = disney_ctx(hd, d);
   const DisneyCtx& C = V.C;
   f3 dir = disney_sample(hd, C, u01(rn.x), u01(rn.y), u01(rn.z));
@@ -121,29 +160,10 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   V.f = f;
   V.brdfPdf = brdfPdf;
   V.ndl = ndl;
-  // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked)
-  const DevTex& E = S.env;
-  int32_t cnt;
-  if ((flags & ER_RENDER_ENV_ALIAS) && S.alias_idx) {
-    // O(1) draw from the search's effective distribution (env.cu):
-    // column from the shared light word, coin from a second word
-    uint32_t coin = philox(make_uint4(idx, sample, 2u + (uint32_t)bounce, 1u), k0, k1).x;
-    int32_t col = (int32_t)__umulhi(rn.w, (uint32_t)(E.w * E.h));
-    cnt = coin < __ldg(S.alias_thresh + col) ? col : __ldg(S.alias_idx + col);
-  } else if (S.env_lut) {
-    cnt = __ldg(S.env_lut + (rn.w >> 8));  // == hdri_search(S.cdf, r1, w*h): r1 = u01(rn.w)
-  } else {
-    cnt = hdri_search(S.cdf, r1, E.w * E.h);
-  }
-  float nu = __fdiv_rn((float)(cnt % E.w), (float)E.w), nv = __fdiv_rn((float)(cnt / E.w), (float)E.h);
-  int32_t ix = __float2int_rz(nu * (float)E.w), iy = __float2int_rz(nv * (float)E.h);
-  ix = __float2int_rz(E.x_tile * ((float)ix - E.x_offset * (float)E.w)) % E.w;
-  iy = __float2int_rz(E.y_tile * ((float)iy - E.y_offset * (float)E.h)) % E.h;
-  float iu = __fdiv_rn((float)ix, (float)E.w), iv = __fdiv_rn((float)iy, (float)E.h);
-  limit_uv(iu, iv);
+  // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked);
+  // the texel (iu, iv) and its value eH were fetched above
   f3 dH = -normalized(reverse_spherical(iu, iv));
-  float hdriPdf = hdri_pdf(S, __float2int_rz(iu * (float)E.w), __float2int_rz(iv * (float)E.h));
-  f3 eH = tex_uv(S, E, iu, iv);
+  float hdriPdf = hdri_pdf(S, eH, ey);
   f3 fH = disney_eval(hd, C, dH);
   float cosH = fabsf(dot(dH, hd.normal));
   f3 hdriC = (fH * cosH) * eH / hdriPdf;
@@ -152,7 +172,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   V.fH = fH;
   V.hdriPdf = hdriPdf;
   V.cosH = cosH;
-  V.env_texel = tex_index(E, __float2int_rz(iu * (float)E.w), __float2int_rz(iv * (float)E.h));
+  V.env_texel = tex_index(E, ex, ey);
   V.env_o = xadd(pos, xscale(dH, 0.001f));
   V.env_d = xnormalize(dH);
   // point light NEE, kernel.cu:175-205
