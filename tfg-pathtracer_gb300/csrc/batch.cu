@@ -366,332 +366,347 @@ er_status render_once(er_batch* b, const er_batch_tuning& t, double* ms, int64_t
 
 extern "C" er_status er_batch_create(er_scene* const* scenes, int32_t n_scenes, const er_scene_opts* opts,
                                      er_batch** out) {
-  if (!out) return fail(ER_ERR_INVALID_ARG, "out is NULL");
-  *out = nullptr;
-  if (!scenes || n_scenes <= 0) return fail(ER_ERR_INVALID_ARG, "no scenes");
-  for (int32_t i = 0; i < n_scenes; i++)
-    if (!scenes[i]) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
-  const int device = scenes[0]->device;
-  for (int32_t i = 0; i < n_scenes; i++)
-    if (scenes[i]->device != device) return fail(ER_ERR_INVALID_ARG, "scenes live on different devices");
-  const bool q8 = opts && opts->bvh_format == ER_BVH_Q8;
-  if (opts && opts->bvh_format != ER_BVH_FP32 && opts->bvh_format != ER_BVH_Q8)
-    return fail(ER_ERR_INVALID_ARG, "bvh_format");
-  if (q8)
+  return guarded("er_batch_create", [&]() -> er_status {
+    if (!out) return fail(ER_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!scenes || n_scenes <= 0) return fail(ER_ERR_INVALID_ARG, "no scenes");
     for (int32_t i = 0; i < n_scenes; i++)
-      if (!scenes[i]->dev.qnodes) return fail(ER_ERR_INVALID_ARG, "ER_BVH_Q8 batch needs scenes built with ER_BVH_Q8");
-  // sizes of each scene's arrays (a scene without triangles still has one slot)
-  int64_t nodes = 0, slots = 0, texels = 0;
-  int64_t mats = 0, texs = 0;
-  bool any_tangents = false;
-  for (int32_t i = 0; i < n_scenes; i++) {
-    const DevScene& S = scenes[i]->dev;
-    nodes += S.n_nodes;
-    slots += std::max<int64_t>(S.n_tris, 1);
-    mats += std::max(S.n_mats, 1);
-    texs += std::max(S.n_texs, 1);
-    texels += scenes[i]->texel_count;
-    any_tangents |= S.tri_t != nullptr;
-  }
-  if (slots > kMaxTris) return fail(ER_ERR_UNSUPPORTED, "merged triangle count exceeds the leaf encoding");
-  if (nodes > 0x7FFFFFFF) return fail(ER_ERR_UNSUPPORTED, "merged node count exceeds int32");
-  ER_CUDA(cudaSetDevice(device));
+      if (!scenes[i]) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+    const int device = scenes[0]->device;
+    for (int32_t i = 0; i < n_scenes; i++)
+      if (scenes[i]->device != device) return fail(ER_ERR_INVALID_ARG, "scenes live on different devices");
+    const bool q8 = opts && opts->bvh_format == ER_BVH_Q8;
+    if (opts && opts->bvh_format != ER_BVH_FP32 && opts->bvh_format != ER_BVH_Q8)
+      return fail(ER_ERR_INVALID_ARG, "bvh_format");
+    if (q8)
+      for (int32_t i = 0; i < n_scenes; i++)
+        if (!scenes[i]->dev.qnodes) return fail(ER_ERR_INVALID_ARG, "ER_BVH_Q8 batch needs scenes built with ER_BVH_Q8");
+    // sizes of each scene's arrays (a scene without triangles still has one slot)
+    int64_t nodes = 0, slots = 0, texels = 0;
+    int64_t mats = 0, texs = 0;
+    bool any_tangents = false;
+    for (int32_t i = 0; i < n_scenes; i++) {
+      const DevScene& S = scenes[i]->dev;
+      nodes += S.n_nodes;
+      slots += std::max<int64_t>(S.n_tris, 1);
+      mats += std::max(S.n_mats, 1);
+      texs += std::max(S.n_texs, 1);
+      texels += scenes[i]->texel_count;
+      any_tangents |= S.tri_t != nullptr;
+    }
+    if (slots > kMaxTris) return fail(ER_ERR_UNSUPPORTED, "merged triangle count exceeds the leaf encoding");
+    if (nodes > 0x7FFFFFFF) return fail(ER_ERR_UNSUPPORTED, "merged node count exceeds int32");
+    ER_CUDA(cudaSetDevice(device));
 
-  er_batch* b = new er_batch();
-  b->device = device;
-  auto bail = [&](er_status e) {
-    er_batch_free(b);
-    return e;
-  };
-  cudaDeviceProp prop;
-  cudaError_t ce = cudaGetDeviceProperties(&prop, device);
-  if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaGetDeviceProperties"));
-  b->num_sms = prop.multiProcessorCount;
-  if (opts && opts->stream) {
-    b->stream = (cudaStream_t)opts->stream;
-  } else {
-    ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaStreamCreate"));
-    b->own_stream = true;
-  }
-  cudaEventCreate(&b->ev0);
-  cudaEventCreate(&b->ev1);
-  b->scenes.assign(scenes, scenes + n_scenes);
-  for (er_scene* s : b->scenes) cudaStreamSynchronize(s->stream);
+    er_batch* b = new er_batch();
+    FreeOnUnwind<er_batch> unwind{b, er_batch_free};
+    b->device = device;
+    auto bail = [&](er_status e) {
+      er_batch_free(b);
+      return e;
+    };
+    cudaDeviceProp prop;
+    cudaError_t ce = cudaGetDeviceProperties(&prop, device);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaGetDeviceProperties"));
+    b->num_sms = prop.multiProcessorCount;
+    if (opts && opts->stream) {
+      b->stream = (cudaStream_t)opts->stream;
+    } else {
+      ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaStreamCreate"));
+      b->own_stream = true;
+    }
+    cudaEventCreate(&b->ev0);
+    cudaEventCreate(&b->ev1);
+    b->scenes.assign(scenes, scenes + n_scenes);
+    for (er_scene* s : b->scenes) cudaStreamSynchronize(s->stream);
 
-  er_status st;
-  void *p_nodes, *p_q = nullptr, *p_tv, *p_tn, *p_tuv, *p_tt = nullptr, *p_mats, *p_texs, *p_texels, *p_err;
-  if ((st = balloc(b, &p_nodes, (size_t)nodes * 128)) != ER_OK) return bail(st);
-  if (q8 && (st = balloc(b, &p_q, (size_t)nodes * 64)) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_tv, (size_t)slots * 48)) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_tn, (size_t)slots * 48)) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_tuv, (size_t)slots * 24)) != ER_OK) return bail(st);
-  if (any_tangents && (st = balloc(b, &p_tt, (size_t)slots * 48)) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_mats, (size_t)mats * sizeof(DevMaterial))) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_texs, (size_t)texs * sizeof(DevTex))) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_texels, (size_t)std::max<int64_t>(texels, 1) * 16)) != ER_OK) return bail(st);
-  if ((st = balloc(b, &p_err, 256)) != ER_OK) return bail(st);
-  ce = cudaMemsetAsync(p_err, 0, 256, b->stream);
-  if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaMemsetAsync"));
-  if (p_tt) {
-    ce = cudaMemsetAsync(p_tt, 0, (size_t)slots * 48, b->stream);
+    er_status st;
+    void *p_nodes, *p_q = nullptr, *p_tv, *p_tn, *p_tuv, *p_tt = nullptr, *p_mats, *p_texs, *p_texels, *p_err;
+    if ((st = balloc(b, &p_nodes, (size_t)nodes * 128)) != ER_OK) return bail(st);
+    if (q8 && (st = balloc(b, &p_q, (size_t)nodes * 64)) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_tv, (size_t)slots * 48)) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_tn, (size_t)slots * 48)) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_tuv, (size_t)slots * 24)) != ER_OK) return bail(st);
+    if (any_tangents && (st = balloc(b, &p_tt, (size_t)slots * 48)) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_mats, (size_t)mats * sizeof(DevMaterial))) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_texs, (size_t)texs * sizeof(DevTex))) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_texels, (size_t)std::max<int64_t>(texels, 1) * 16)) != ER_OK) return bail(st);
+    if ((st = balloc(b, &p_err, 256)) != ER_OK) return bail(st);
+    ce = cudaMemsetAsync(p_err, 0, 256, b->stream);
     if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaMemsetAsync"));
-  }
+    if (p_tt) {
+      ce = cudaMemsetAsync(p_tt, 0, (size_t)slots * 48, b->stream);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaMemsetAsync"));
+    }
 
-  int64_t nb = 0, sb = 0, tb = 0;
-  int32_t mb = 0, xb = 0;
-  float eps = 0;
-  auto cp = [&](void* dst, const void* src, size_t bytes) {
-    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, b->stream) : cudaSuccess;
-  };
-  for (int32_t i = 0; i < n_scenes; i++) {
-    const er_scene* sc = b->scenes[i];
-    const DevScene& S = sc->dev;
-    const int64_t ns = std::max<int64_t>(S.n_tris, 1);
-    const int32_t nm = std::max(S.n_mats, 1), nt = std::max(S.n_texs, 1);
-    char* c_nodes = (char*)p_nodes + nb * 128;
-    char* c_tv = (char*)p_tv + sb * 48;
-    char* c_mats = (char*)p_mats + (size_t)mb * sizeof(DevMaterial);
-    char* c_texs = (char*)p_texs + (size_t)xb * sizeof(DevTex);
-    cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess) e = cp(c_nodes, S.nodes, (size_t)S.n_nodes * 128);
-    if (e == cudaSuccess && q8) e = cp((char*)p_q + nb * 64, S.qnodes, (size_t)S.n_nodes * 64);
-    if (e == cudaSuccess) e = cp(c_tv, S.tri_v, (size_t)ns * 48);
-    if (e == cudaSuccess) e = cp((char*)p_tn + sb * 48, S.tri_n, (size_t)ns * 48);
-    if (e == cudaSuccess) e = cp((char*)p_tuv + sb * 24, S.tri_uv, (size_t)ns * 24);
-    if (e == cudaSuccess && S.tri_t) e = cp((char*)p_tt + sb * 48, S.tri_t, (size_t)ns * 48);
-    if (e == cudaSuccess) e = cp(c_mats, S.mats, (size_t)nm * sizeof(DevMaterial));
-    if (e == cudaSuccess) e = cp(c_texs, S.texs, (size_t)nt * sizeof(DevTex));
-    if (e == cudaSuccess) e = cp((char*)p_texels + tb * 16, S.texels, (size_t)sc->texel_count * 16);
-    if (e != cudaSuccess) return bail(cuda_fail(e, "batch merge copy"));
-    k_fix_nodes<<<blocks(S.n_nodes), 256, 0, b->stream>>>((float4*)c_nodes, S.n_nodes, (int32_t)nb, (int32_t)sb);
-    if (q8) k_fix_qnodes<<<blocks(S.n_nodes), 256, 0, b->stream>>>((uint4*)((char*)p_q + nb * 64), S.n_nodes,
-                                                                    (int32_t)nb, (int32_t)sb);
-    k_fix_tri_mat<<<blocks(ns), 256, 0, b->stream>>>((float4*)c_tv, ns, mb);
-    k_fix_mats<<<blocks(nm), 256, 0, b->stream>>>((DevMaterial*)c_mats, nm, xb);
-    k_fix_texs<<<blocks(nt), 256, 0, b->stream>>>((DevTex*)c_texs, nt, tb);
-    ce = cudaGetLastError();
-    if (ce != cudaSuccess) return bail(cuda_fail(ce, "batch fix-up"));
-    b->root.push_back((int32_t)nb);
-    b->texel_base.push_back(tb);
-    eps = std::max(eps, S.scene_eps);
-    nb += S.n_nodes;
-    sb += ns;
-    mb += nm;
-    xb += nt;
-    tb += sc->texel_count;
-  }
-  ce = cudaStreamSynchronize(b->stream);
-  if (ce != cudaSuccess) return bail(cuda_fail(ce, "batch merge"));
+    int64_t nb = 0, sb = 0, tb = 0;
+    int32_t mb = 0, xb = 0;
+    float eps = 0;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+      return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, b->stream) : cudaSuccess;
+    };
+    for (int32_t i = 0; i < n_scenes; i++) {
+      const er_scene* sc = b->scenes[i];
+      const DevScene& S = sc->dev;
+      const int64_t ns = std::max<int64_t>(S.n_tris, 1);
+      const int32_t nm = std::max(S.n_mats, 1), nt = std::max(S.n_texs, 1);
+      char* c_nodes = (char*)p_nodes + nb * 128;
+      char* c_tv = (char*)p_tv + sb * 48;
+      char* c_mats = (char*)p_mats + (size_t)mb * sizeof(DevMaterial);
+      char* c_texs = (char*)p_texs + (size_t)xb * sizeof(DevTex);
+      cudaError_t e = cudaSuccess;
+      if (e == cudaSuccess) e = cp(c_nodes, S.nodes, (size_t)S.n_nodes * 128);
+      if (e == cudaSuccess && q8) e = cp((char*)p_q + nb * 64, S.qnodes, (size_t)S.n_nodes * 64);
+      if (e == cudaSuccess) e = cp(c_tv, S.tri_v, (size_t)ns * 48);
+      if (e == cudaSuccess) e = cp((char*)p_tn + sb * 48, S.tri_n, (size_t)ns * 48);
+      if (e == cudaSuccess) e = cp((char*)p_tuv + sb * 24, S.tri_uv, (size_t)ns * 24);
+      if (e == cudaSuccess && S.tri_t) e = cp((char*)p_tt + sb * 48, S.tri_t, (size_t)ns * 48);
+      if (e == cudaSuccess) e = cp(c_mats, S.mats, (size_t)nm * sizeof(DevMaterial));
+      if (e == cudaSuccess) e = cp(c_texs, S.texs, (size_t)nt * sizeof(DevTex));
+      if (e == cudaSuccess) e = cp((char*)p_texels + tb * 16, S.texels, (size_t)sc->texel_count * 16);
+      if (e != cudaSuccess) return bail(cuda_fail(e, "batch merge copy"));
+      k_fix_nodes<<<blocks(S.n_nodes), 256, 0, b->stream>>>((float4*)c_nodes, S.n_nodes, (int32_t)nb, (int32_t)sb);
+      if (q8) k_fix_qnodes<<<blocks(S.n_nodes), 256, 0, b->stream>>>((uint4*)((char*)p_q + nb * 64), S.n_nodes,
+                                                                      (int32_t)nb, (int32_t)sb);
+      k_fix_tri_mat<<<blocks(ns), 256, 0, b->stream>>>((float4*)c_tv, ns, mb);
+      k_fix_mats<<<blocks(nm), 256, 0, b->stream>>>((DevMaterial*)c_mats, nm, xb);
+      k_fix_texs<<<blocks(nt), 256, 0, b->stream>>>((DevTex*)c_texs, nt, tb);
+      ce = cudaGetLastError();
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "batch fix-up"));
+      b->root.push_back((int32_t)nb);
+      b->texel_base.push_back(tb);
+      eps = std::max(eps, S.scene_eps);
+      nb += S.n_nodes;
+      sb += ns;
+      mb += nm;
+      xb += nt;
+      tb += sc->texel_count;
+    }
+    ce = cudaStreamSynchronize(b->stream);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "batch merge"));
 
-  DevScene& M = b->dev;
-  M = b->scenes[0]->dev;  // per-job parts (env, lights, camera) come from the job table
-  M.nodes = (const float4*)p_nodes;
-  M.qnodes = (const uint4*)p_q;
-  M.tri_v = (const float4*)p_tv;
-  M.tri_n = (const float4*)p_tn;
-  M.tri_uv = (const float2*)p_tuv;
-  M.tri_t = (const float4*)p_tt;
-  M.mats = (const DevMaterial*)p_mats;
-  M.texs = (const DevTex*)p_texs;
-  M.texels = (const float4*)p_texels;
-  M.env.offset += b->texel_base[0];
-  M.n_mats = (int32_t)mats;
-  M.n_texs = (int32_t)texs;
-  M.n_tris = slots;
-  M.n_nodes = nodes;
-  M.scene_eps = eps;
-  M.use_q8 = q8;
-  b->err_word = (uint32_t*)p_err;
-  b->d_stats = (unsigned long long*)((char*)p_err + 64);
-  // occupancy queries of the batch kernels, outside any stream capture
-  std::vector<BatchWave> none;
-  if ((st = batch_launch(M, nullptr, nullptr, nullptr, none, BatchSchedule{}, b->num_sms, b->err_word, b->stream,
-                         nullptr)) != ER_OK)
-    return bail(st);
-  *out = b;
-  return ER_OK;
+    DevScene& M = b->dev;
+    M = b->scenes[0]->dev;  // per-job parts (env, lights, camera) come from the job table
+    M.nodes = (const float4*)p_nodes;
+    M.qnodes = (const uint4*)p_q;
+    M.tri_v = (const float4*)p_tv;
+    M.tri_n = (const float4*)p_tn;
+    M.tri_uv = (const float2*)p_tuv;
+    M.tri_t = (const float4*)p_tt;
+    M.mats = (const DevMaterial*)p_mats;
+    M.texs = (const DevTex*)p_texs;
+    M.texels = (const float4*)p_texels;
+    M.env.offset += b->texel_base[0];
+    M.n_mats = (int32_t)mats;
+    M.n_texs = (int32_t)texs;
+    M.n_tris = slots;
+    M.n_nodes = nodes;
+    M.scene_eps = eps;
+    M.use_q8 = q8;
+    b->err_word = (uint32_t*)p_err;
+    b->d_stats = (unsigned long long*)((char*)p_err + 64);
+    // occupancy queries of the batch kernels, outside any stream capture
+    std::vector<BatchWave> none;
+    if ((st = batch_launch(M, nullptr, nullptr, nullptr, none, BatchSchedule{}, b->num_sms, b->err_word, b->stream,
+                           nullptr)) != ER_OK)
+      return bail(st);
+    *out = b;
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_batch_set_jobs(er_batch* b, const er_batch_job* jobs, int32_t n_jobs) {
-  if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
-  if (n_jobs < 0 || (n_jobs > 0 && !jobs)) return fail(ER_ERR_INVALID_ARG, "bad job list");
-  for (int32_t j = 0; j < n_jobs; j++) {
-    const er_batch_job& J = jobs[j];
-    if (J.scene < 0 || J.scene >= (int32_t)b->scenes.size()) return fail(ER_ERR_INVALID_ARG, "job scene out of range");
-    er_status cs = validate_camera(J.camera);
-    if (cs != ER_OK) return fail(cs, "job " + std::to_string(j) + ": " + er_last_error());
-    if (J.spp < 0 || J.sample_begin < 0 || J.max_depth < 0 || J.max_depth > 64)
-      return fail(ER_ERR_INVALID_ARG, "job options out of range");
-    if (J.flags & ~(uint32_t)(ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64))
-      return fail(ER_ERR_INVALID_ARG, "job flags: only ER_RENDER_ENV_ALIAS and ER_RENDER_ACCUM_FP64");
-  }
-  ER_CUDA(cudaSetDevice(b->device));
-  drop_jobs(b);
-  er_status st;
-  std::vector<BatchJobDev> table((size_t)n_jobs);
-  b->films.resize((size_t)n_jobs);
-  for (int32_t j = 0; j < n_jobs; j++) {
-    const er_batch_job& J = jobs[j];
-    er_scene* sc = b->scenes[(size_t)J.scene];
-    if ((J.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(sc)) != ER_OK) return st;
-    if ((st = build_env_lut(sc)) != ER_OK) return st;
-    Film& F = b->films[(size_t)j];
-    F.w = J.camera.x_res;
-    F.h = J.camera.y_res;
-    const size_t np = (size_t)F.w * F.h;
-    if ((st = balloc(b, (void**)&F.beauty, np * sizeof(float4))) != ER_OK) return st;
-    if ((st = balloc(b, (void**)&F.samples, np * 4)) != ER_OK) return st;
-    if ((st = balloc(b, (void**)&F.pathcount, np * 4)) != ER_OK) return st;
-    if ((J.flags & ER_RENDER_ACCUM_FP64) && (st = balloc(b, (void**)&F.sum, np * 3 * sizeof(double))) != ER_OK)
-      return st;
-    BatchJobDev& D = table[(size_t)j];
-    std::memset(&D, 0, sizeof D);
-    const DevScene& S = sc->dev;
-    D.env = S.env;
-    D.env.offset += b->texel_base[(size_t)J.scene];
-    D.cdf = S.cdf;
-    D.alias_idx = S.alias_idx;
-    D.alias_thresh = S.alias_thresh;
-    D.env_lut = S.env_lut;
-    D.lights = S.lights;
-    D.radiance_sum = S.radiance_sum;
-    D.n_lights = S.n_lights;
-    D.root = b->root[(size_t)J.scene];
-    D.scene_eps = S.scene_eps;
-    D.cam = make_dev_camera(J.camera);
-    D.film = F;
-  }
-  b->jobs.assign(jobs, jobs + n_jobs);
-  if (n_jobs > 0) {
-    if ((st = balloc(b, (void**)&b->d_jobs, table.size() * sizeof(BatchJobDev))) != ER_OK) return st;
-    ER_CUDA(cudaMemcpyAsync(b->d_jobs, table.data(), table.size() * sizeof(BatchJobDev), cudaMemcpyHostToDevice,
-                            b->stream));
-    ER_CUDA(cudaStreamSynchronize(b->stream));
-  }
-  return ER_OK;
+  return guarded("er_batch_set_jobs", [&]() -> er_status {
+    if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
+    if (n_jobs < 0 || (n_jobs > 0 && !jobs)) return fail(ER_ERR_INVALID_ARG, "bad job list");
+    for (int32_t j = 0; j < n_jobs; j++) {
+      const er_batch_job& J = jobs[j];
+      if (J.scene < 0 || J.scene >= (int32_t)b->scenes.size()) return fail(ER_ERR_INVALID_ARG, "job scene out of range");
+      er_status cs = validate_camera(J.camera);
+      if (cs != ER_OK) return fail(cs, "job " + std::to_string(j) + ": " + er_last_error());
+      if (J.spp < 0 || J.sample_begin < 0 || J.max_depth < 0 || J.max_depth > 64)
+        return fail(ER_ERR_INVALID_ARG, "job options out of range");
+      if (J.flags & ~(uint32_t)(ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64))
+        return fail(ER_ERR_INVALID_ARG, "job flags: only ER_RENDER_ENV_ALIAS and ER_RENDER_ACCUM_FP64");
+    }
+    ER_CUDA(cudaSetDevice(b->device));
+    drop_jobs(b);
+    er_status st;
+    std::vector<BatchJobDev> table((size_t)n_jobs);
+    b->films.resize((size_t)n_jobs);
+    for (int32_t j = 0; j < n_jobs; j++) {
+      const er_batch_job& J = jobs[j];
+      er_scene* sc = b->scenes[(size_t)J.scene];
+      if ((J.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(sc)) != ER_OK) return st;
+      if ((st = build_env_lut(sc)) != ER_OK) return st;
+      Film& F = b->films[(size_t)j];
+      F.w = J.camera.x_res;
+      F.h = J.camera.y_res;
+      const size_t np = (size_t)F.w * F.h;
+      if ((st = balloc(b, (void**)&F.beauty, np * sizeof(float4))) != ER_OK) return st;
+      if ((st = balloc(b, (void**)&F.samples, np * 4)) != ER_OK) return st;
+      if ((st = balloc(b, (void**)&F.pathcount, np * 4)) != ER_OK) return st;
+      if ((J.flags & ER_RENDER_ACCUM_FP64) && (st = balloc(b, (void**)&F.sum, np * 3 * sizeof(double))) != ER_OK)
+        return st;
+      BatchJobDev& D = table[(size_t)j];
+      std::memset(&D, 0, sizeof D);
+      const DevScene& S = sc->dev;
+      D.env = S.env;
+      D.env.offset += b->texel_base[(size_t)J.scene];
+      D.cdf = S.cdf;
+      D.alias_idx = S.alias_idx;
+      D.alias_thresh = S.alias_thresh;
+      D.env_lut = S.env_lut;
+      D.lights = S.lights;
+      D.radiance_sum = S.radiance_sum;
+      D.n_lights = S.n_lights;
+      D.root = b->root[(size_t)J.scene];
+      D.scene_eps = S.scene_eps;
+      D.cam = make_dev_camera(J.camera);
+      D.film = F;
+    }
+    b->jobs.assign(jobs, jobs + n_jobs);
+    if (n_jobs > 0) {
+      if ((st = balloc(b, (void**)&b->d_jobs, table.size() * sizeof(BatchJobDev))) != ER_OK) return st;
+      ER_CUDA(cudaMemcpyAsync(b->d_jobs, table.data(), table.size() * sizeof(BatchJobDev), cudaMemcpyHostToDevice,
+                              b->stream));
+      ER_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_batch_render(er_batch* b, const er_batch_tuning* tuning, er_render_stats* stats) {
-  if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
-  ER_CUDA(cudaSetDevice(b->device));
-  if (b->jobs.empty()) return fail(ER_ERR_INVALID_ARG, "no jobs (er_batch_set_jobs)");
-  er_batch_tuning t = tuning ? *tuning : (b->has_tuned ? b->tuned : default_tuning());
-  if (t.wave_paths < 0 || t.trace_blocks_per_sm < 0 || t.shade_blocks_per_sm < 0)
-    return fail(ER_ERR_INVALID_ARG, "tuning out of range");
-  unsigned long long st0[8], st1[8];
-  ER_CUDA(cudaMemcpyAsync(st0, b->d_stats, sizeof st0, cudaMemcpyDeviceToHost, b->stream));
-  ER_CUDA(cudaStreamSynchronize(b->stream));
-  double ms = 0;
-  int64_t nl = 0;
-  er_status st = render_once(b, t, &ms, &nl);
-  if (st != ER_OK) return st;
-  if (stats) {
-    ER_CUDA(cudaMemcpy(st1, b->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
-    std::memset(stats, 0, sizeof *stats);
-    stats->ms = ms;
-    for (const er_batch_job& J : b->jobs) stats->samples += (int64_t)J.spp * job_npix(J);
-    stats->rays_closest = (int64_t)(st1[0] - st0[0]);
-    stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
-    stats->path_vertices = (int64_t)(st1[6] - st0[6]);
-    stats->kernel_launches = nl;
-  }
-  return ER_OK;
+  return guarded("er_batch_render", [&]() -> er_status {
+    if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
+    ER_CUDA(cudaSetDevice(b->device));
+    if (b->jobs.empty()) return fail(ER_ERR_INVALID_ARG, "no jobs (er_batch_set_jobs)");
+    er_batch_tuning t = tuning ? *tuning : (b->has_tuned ? b->tuned : default_tuning());
+    if (t.wave_paths < 0 || t.trace_blocks_per_sm < 0 || t.shade_blocks_per_sm < 0)
+      return fail(ER_ERR_INVALID_ARG, "tuning out of range");
+    unsigned long long st0[8], st1[8];
+    ER_CUDA(cudaMemcpyAsync(st0, b->d_stats, sizeof st0, cudaMemcpyDeviceToHost, b->stream));
+    ER_CUDA(cudaStreamSynchronize(b->stream));
+    double ms = 0;
+    int64_t nl = 0;
+    er_status st = render_once(b, t, &ms, &nl);
+    if (st != ER_OK) return st;
+    if (stats) {
+      ER_CUDA(cudaMemcpy(st1, b->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
+      std::memset(stats, 0, sizeof *stats);
+      stats->ms = ms;
+      for (const er_batch_job& J : b->jobs) stats->samples += (int64_t)J.spp * job_npix(J);
+      stats->rays_closest = (int64_t)(st1[0] - st0[0]);
+      stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
+      stats->path_vertices = (int64_t)(st1[6] - st0[6]);
+      stats->kernel_launches = nl;
+    }
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_batch_read(er_batch* b, int32_t job, uint32_t flags, float* beauty, uint32_t* samples,
                                    uint32_t* pathcount) {
-  if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
-  if (job < 0 || job >= (int32_t)b->films.size()) return fail(ER_ERR_INVALID_ARG, "job out of range");
-  ER_CUDA(cudaSetDevice(b->device));
-  const Film& F = b->films[(size_t)job];
-  const size_t np = (size_t)F.w * F.h;
-  const cudaMemcpyKind k = (flags & ER_RENDER_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  if (beauty) ER_CUDA(cudaMemcpyAsync(beauty, F.beauty, np * sizeof(float4), k, b->stream));
-  if (samples) ER_CUDA(cudaMemcpyAsync(samples, F.samples, np * 4, k, b->stream));
-  if (pathcount) ER_CUDA(cudaMemcpyAsync(pathcount, F.pathcount, np * 4, k, b->stream));
-  ER_CUDA(cudaStreamSynchronize(b->stream));
-  return ER_OK;
+  return guarded("er_batch_read", [&]() -> er_status {
+    if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
+    if (job < 0 || job >= (int32_t)b->films.size()) return fail(ER_ERR_INVALID_ARG, "job out of range");
+    ER_CUDA(cudaSetDevice(b->device));
+    const Film& F = b->films[(size_t)job];
+    const size_t np = (size_t)F.w * F.h;
+    const cudaMemcpyKind k = (flags & ER_RENDER_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (beauty) ER_CUDA(cudaMemcpyAsync(beauty, F.beauty, np * sizeof(float4), k, b->stream));
+    if (samples) ER_CUDA(cudaMemcpyAsync(samples, F.samples, np * 4, k, b->stream));
+    if (pathcount) ER_CUDA(cudaMemcpyAsync(pathcount, F.pathcount, np * 4, k, b->stream));
+    ER_CUDA(cudaStreamSynchronize(b->stream));
+    return ER_OK;
+  });
 }
 
 // Coordinate descent over the schedule knobs, each candidate timed as the
 // best of `reps` graph replays of the current jobs.
 extern "C" er_status er_batch_autotune(er_batch* b, int32_t reps, er_batch_tuning* best) {
-  if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
-  ER_CUDA(cudaSetDevice(b->device));
-  if (b->jobs.empty()) return fail(ER_ERR_INVALID_ARG, "no jobs (er_batch_set_jobs)");
-  reps = std::max(1, reps);
-  auto measure = [&](const er_batch_tuning& t, double* out) -> er_status {
-    double m = 1e300;
-    for (int32_t r = 0; r <= reps; r++) {  // first run builds the graph
-      double ms = 0;
-      er_status st = render_once(b, t, &ms, nullptr);
-      if (st != ER_OK) return st;
-      if (r > 0) m = std::min(m, ms);
-    }
-    *out = m;
-    return ER_OK;
-  };
-  er_batch_tuning cur = default_tuning();
-  double cur_ms = 0;
-  er_status st = measure(cur, &cur_ms);
-  if (st != ER_OK) return st;
-  auto try_knob = [&](auto set, std::initializer_list<int32_t> values) -> er_status {
-    er_batch_tuning bestt = cur;
-    double best_ms = cur_ms;
-    for (int32_t v : values) {
-      er_batch_tuning t = cur;
-      set(t, v);
-      if (same_tuning(t, cur)) continue;
-      double ms = 0;
-      er_status e = measure(t, &ms);
-      if (e != ER_OK) return e;
-      if (ms < best_ms) {
-        best_ms = ms;
-        bestt = t;
+  return guarded("er_batch_autotune", [&]() -> er_status {
+    if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
+    ER_CUDA(cudaSetDevice(b->device));
+    if (b->jobs.empty()) return fail(ER_ERR_INVALID_ARG, "no jobs (er_batch_set_jobs)");
+    reps = std::max(1, reps);
+    auto measure = [&](const er_batch_tuning& t, double* out) -> er_status {
+      double m = 1e300;
+      for (int32_t r = 0; r <= reps; r++) {  // first run builds the graph
+        double ms = 0;
+        er_status st = render_once(b, t, &ms, nullptr);
+        if (st != ER_OK) return st;
+        if (r > 0) m = std::min(m, ms);
       }
-    }
-    cur = bestt;
-    cur_ms = best_ms;
+      *out = m;
+      return ER_OK;
+    };
+    er_batch_tuning cur = default_tuning();
+    double cur_ms = 0;
+    er_status st = measure(cur, &cur_ms);
+    if (st != ER_OK) return st;
+    auto try_knob = [&](auto set, std::initializer_list<int32_t> values) -> er_status {
+      er_batch_tuning bestt = cur;
+      double best_ms = cur_ms;
+      for (int32_t v : values) {
+        er_batch_tuning t = cur;
+        set(t, v);
+        if (same_tuning(t, cur)) continue;
+        double ms = 0;
+        er_status e = measure(t, &ms);
+        if (e != ER_OK) return e;
+        if (ms < best_ms) {
+          best_ms = ms;
+          bestt = t;
+        }
+      }
+      cur = bestt;
+      cur_ms = best_ms;
+      return ER_OK;
+    };
+    if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.wave_paths = v; },
+                       {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24})) != ER_OK)
+      return st;
+    if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.trace_blocks_per_sm = v; }, {0, 4, 5, 6})) != ER_OK)
+      return st;
+    if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.shade_blocks_per_sm = v; }, {0, 4, 8})) != ER_OK)
+      return st;
+    if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.split_trace = v; }, {0, 1})) != ER_OK) return st;
+    if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.one_stream = v; }, {0, 1})) != ER_OK) return st;
+    b->tuned = cur;
+    b->has_tuned = true;
+    if (best) *best = cur;
     return ER_OK;
-  };
-  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.wave_paths = v; },
-                     {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24})) != ER_OK)
-    return st;
-  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.trace_blocks_per_sm = v; }, {0, 4, 5, 6})) != ER_OK)
-    return st;
-  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.shade_blocks_per_sm = v; }, {0, 4, 8})) != ER_OK)
-    return st;
-  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.split_trace = v; }, {0, 1})) != ER_OK) return st;
-  if ((st = try_knob([](er_batch_tuning& t, int32_t v) { t.one_stream = v; }, {0, 1})) != ER_OK) return st;
-  b->tuned = cur;
-  b->has_tuned = true;
-  if (best) *best = cur;
-  return ER_OK;
+  });
 }
 
 extern "C" er_status er_batch_info(const er_batch* b, int32_t* n_waves, int64_t* device_bytes) {
-  if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
-  if (n_waves) *n_waves = (int32_t)b->waves.size();
-  if (device_bytes) *device_bytes = b->device_bytes;
-  return ER_OK;
+  return guarded("er_batch_info", [&]() -> er_status {
+    if (!b) return fail(ER_ERR_INVALID_ARG, "batch is NULL");
+    if (n_waves) *n_waves = (int32_t)b->waves.size();
+    if (device_bytes) *device_bytes = b->device_bytes;
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_batch_free(er_batch* b) {
-  if (!b) return ER_OK;
-  cudaSetDevice(b->device);
-  if (b->stream) cudaStreamSynchronize(b->stream);
-  drop_graph(b);
-  if (b->pair.s2) cudaStreamSynchronize(b->pair.s2);
-  wave_destroy(b->wave);
-  wave_destroy(b->pair.w2);
-  for (void* p : b->allocs) cudaFree(p);
-  if (b->pair.s2) cudaStreamDestroy(b->pair.s2);
-  for (cudaEvent_t e : {b->pair.ev_fork, b->pair.ev_join, b->pair.ev_acc[0], b->pair.ev_acc[1]})
-    if (e) cudaEventDestroy(e);
-  if (b->ev0) cudaEventDestroy(b->ev0);
-  if (b->ev1) cudaEventDestroy(b->ev1);
-  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
-  delete b;
-  return ER_OK;
+  return guarded("er_batch_free", [&]() -> er_status {
+    if (!b) return ER_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    if (b->pair.s2) cudaStreamSynchronize(b->pair.s2);
+    wave_destroy(b->wave);
+    wave_destroy(b->pair.w2);
+    for (void* p : b->allocs) cudaFree(p);
+    if (b->pair.s2) cudaStreamDestroy(b->pair.s2);
+    for (cudaEvent_t e : {b->pair.ev_fork, b->pair.ev_join, b->pair.ev_acc[0], b->pair.ev_acc[1]})
+      if (e) cudaEventDestroy(e);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return ER_OK;
+  });
 }

@@ -155,26 +155,30 @@ extern "C" int32_t er_abi_version(void) { return ER_ABI_VERSION; }
 
 // main.cpp:99 (clampPixels, PostProcessing.cpp:30-33) then main.cpp:156-158
 extern "C" er_status er_encode_ldr(const float* rgba, int32_t width, int32_t height, uint8_t* out) {
-  if (!rgba || !out || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARG, "bad image arguments");
-  size_t n = (size_t)width * height * 4;
-  for (size_t i = 0; i < n; i++) {
-    float v = rgba[i];
-    v = v < 0.0f ? 0.0f : v > 1.0f ? 1.0f : v;  // Math.hpp:30-32 clamp, NaN kept
-    double e = fast_pow((double)v, 1.0 / 2.2) * 255.0;
-    if (!(e >= 0.0 && e < 256.0)) e = 0.0;  // NaN input: defined as 0
-    out[i] = (uint8_t)(int32_t)e;
-  }
-  return ER_OK;
+  return guarded("er_encode_ldr", [&]() -> er_status {
+    if (!rgba || !out || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARG, "bad image arguments");
+    size_t n = (size_t)width * height * 4;
+    for (size_t i = 0; i < n; i++) {
+      float v = rgba[i];
+      v = v < 0.0f ? 0.0f : v > 1.0f ? 1.0f : v;  // Math.hpp:30-32 clamp, NaN kept
+      double e = fast_pow((double)v, 1.0 / 2.2) * 255.0;
+      if (!(e >= 0.0 && e < 256.0)) e = 0.0;  // NaN input: defined as 0
+      out[i] = (uint8_t)(int32_t)e;
+    }
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_write_image(const char* path, const uint8_t* rgba, int32_t width, int32_t height,
                                     int32_t as_bmp) {
-  if (!path || !rgba || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARG, "bad image arguments");
-  std::vector<uint8_t> bytes = as_bmp ? encode_bmp(rgba, width, height) : encode_png(rgba, width, height);
-  FILE* f = std::fopen(path, "wb");
-  if (!f) return fail(ER_ERR_IO, std::string("cannot open ") + path);
-  size_t wr = std::fwrite(bytes.data(), 1, bytes.size(), f);
-  int rc = std::fclose(f);
-  if (wr != bytes.size() || rc != 0) return fail(ER_ERR_IO, std::string("write failed: ") + path);
-  return ER_OK;
+  return guarded("er_write_image", [&]() -> er_status {
+    if (!path || !rgba || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARG, "bad image arguments");
+    std::vector<uint8_t> bytes = as_bmp ? encode_bmp(rgba, width, height) : encode_png(rgba, width, height);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(ER_ERR_IO, std::string("cannot open ") + path);
+    size_t wr = std::fwrite(bytes.data(), 1, bytes.size(), f);
+    int rc = std::fclose(f);
+    if (wr != bytes.size() || rc != 0) return fail(ER_ERR_IO, std::string("write failed: ") + path);
+    return ER_OK;
+  });
 }

@@ -134,26 +134,30 @@ er_status build_env_alias(er_scene* s) {
 using namespace er;
 
 extern "C" er_status er_env_search_table(er_scene* s, int32_t* table) {
-  if (!s || !table) return fail(ER_ERR_INVALID_ARG, "NULL argument");
-  ER_CUDA(cudaSetDevice(s->device));
-  if ((int64_t)s->dev.env.w * s->dev.env.h < kEnvLutMinTexels)
-    return fail(ER_ERR_INVALID_ARG, "environment below the table threshold: sampled by the search");
-  er_status st = build_env_lut(s);
-  if (st != ER_OK) return st;
-  ER_CUDA(cudaMemcpyAsync(table, s->env_lut_buf, (size_t)kGrid * 4, cudaMemcpyDeviceToHost, s->stream));
-  ER_CUDA(cudaStreamSynchronize(s->stream));
-  return ER_OK;
+  return guarded("er_env_search_table", [&]() -> er_status {
+    if (!s || !table) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+    ER_CUDA(cudaSetDevice(s->device));
+    if ((int64_t)s->dev.env.w * s->dev.env.h < kEnvLutMinTexels)
+      return fail(ER_ERR_INVALID_ARG, "environment below the table threshold: sampled by the search");
+    er_status st = build_env_lut(s);
+    if (st != ER_OK) return st;
+    ER_CUDA(cudaMemcpyAsync(table, s->env_lut_buf, (size_t)kGrid * 4, cudaMemcpyDeviceToHost, s->stream));
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_env_distribution(er_scene* s, uint32_t* counts, int32_t* alias, uint32_t* thresh) {
-  if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
-  ER_CUDA(cudaSetDevice(s->device));
-  er_status st = build_env_alias(s);
-  if (st != ER_OK) return st;
-  const size_t n = (size_t)s->dev.env.w * s->dev.env.h;
-  if (counts) ER_CUDA(cudaMemcpyAsync(counts, s->env_counts, n * 4, cudaMemcpyDeviceToHost, s->stream));
-  if (alias) ER_CUDA(cudaMemcpyAsync(alias, s->dev.alias_idx, n * 4, cudaMemcpyDeviceToHost, s->stream));
-  if (thresh) ER_CUDA(cudaMemcpyAsync(thresh, s->dev.alias_thresh, n * 4, cudaMemcpyDeviceToHost, s->stream));
-  ER_CUDA(cudaStreamSynchronize(s->stream));
-  return ER_OK;
+  return guarded("er_env_distribution", [&]() -> er_status {
+    if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+    ER_CUDA(cudaSetDevice(s->device));
+    er_status st = build_env_alias(s);
+    if (st != ER_OK) return st;
+    const size_t n = (size_t)s->dev.env.w * s->dev.env.h;
+    if (counts) ER_CUDA(cudaMemcpyAsync(counts, s->env_counts, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    if (alias) ER_CUDA(cudaMemcpyAsync(alias, s->dev.alias_idx, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    if (thresh) ER_CUDA(cudaMemcpyAsync(thresh, s->dev.alias_thresh, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    return ER_OK;
+  });
 }

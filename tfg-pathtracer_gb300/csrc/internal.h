@@ -4,7 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <exception>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -17,6 +20,42 @@ namespace er {
 void set_error(const std::string& msg);
 er_status fail(er_status s, const std::string& msg);
 er_status cuda_fail(cudaError_t e, const char* what);
+
+// Runs the body of a C-ABI entry point: a C++ exception (a host allocation
+// that failed, a container size out of range) becomes a status instead of
+// crossing the C ABI.
+template <typename F>
+er_status guarded(const char* what, F&& body) noexcept {
+  er_status s = ER_ERR_INVALID_ARG;
+  const char* why = "unexpected exception";
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    s = ER_ERR_OOM;
+    why = "host memory allocation failed";
+  } catch (const std::length_error&) {
+    s = ER_ERR_OOM;
+    why = "host buffer size out of range";
+  } catch (...) {
+  }
+  try {
+    fail(s, std::string(what) + ": " + why);
+  } catch (...) {  // no memory left for the message either
+  }
+  return s;
+}
+
+// Frees a half-built handle when an exception unwinds past it (guarded()
+// then reports it); the error returns free it themselves.
+template <typename T>
+struct FreeOnUnwind {
+  T* h;
+  er_status (*free_fn)(T*);
+  int n = std::uncaught_exceptions();
+  ~FreeOnUnwind() {
+    if (std::uncaught_exceptions() > n) free_fn(h);
+  }
+};
 
 #define ER_CUDA(call)                                        \
   do {                                                       \

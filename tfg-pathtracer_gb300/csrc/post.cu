@@ -118,96 +118,98 @@ using namespace er;
 
 extern "C" er_status er_postprocess(const float* rgba_in, int32_t width, int32_t height, const er_post_opts* opts,
                                     float* rgba_out, uint8_t* ldr_out, uint32_t flags) {
-  if (!rgba_in || width <= 0 || height <= 0 || (!rgba_out && !ldr_out))
-    return fail(ER_ERR_INVALID_ARG, "bad post-processing arguments");
-  if ((int64_t)width * height > ((int64_t)1 << 28)) return fail(ER_ERR_INVALID_ARG, "image too large");
-  er_post_opts o{};
-  o.exposure = 1.0f;
-  if (opts) o = *opts;
-  if (o.tonemap < ER_TONEMAP_NONE || o.tonemap > ER_TONEMAP_ACES) return fail(ER_ERR_INVALID_ARG, "tonemap");
-  if (o.bloom_power != 0.0f && !(o.bloom_radius >= 0.0f && o.bloom_radius <= 256.0f))
-    return fail(ER_ERR_INVALID_ARG, "bloom radius out of range");
-  int dev = 0;
-  ER_CUDA(cudaGetDevice(&dev));
-  const bool devp = flags & ER_RENDER_DEVICE_OUT;
-  const size_t n = (size_t)width * height;
-  PostParams P;
-  P.w = width;
-  P.h = height;
-  P.exposure = o.exposure;
-  P.tonemap = o.tonemap;
-  P.clamp01 = o.clamp != 0;
-  P.srgb = o.srgb != 0;
-  P.flip_x = o.flip_x != 0;
-  P.flip_y = o.flip_y != 0;
-  P.threshold = o.bloom_threshold;
-  P.power = o.bloom_power;
-  P.blur = o.bloom_power != 0.0f ? (int32_t)(o.bloom_radius / 2) : 0;
-  // basicBlur's kernel (PostProcessing.cpp:144-152), built on the host
-  const int32_t ks = 2 * P.blur + 1;
-  std::vector<float> kern(P.blur > 0 ? (size_t)ks * ks : 1, 0.0f);
-  if (P.blur > 0) {
-    const float sd = o.bloom_radius;
-    const float kernelSize = (float)ks;
-    for (int32_t x = 0; x < ks; x++)
-      for (int32_t y = 0; y < ks; y++) {
-        float t1 = (float)(1.0 / ((2.0 * (double)3.14159265358979323846f) * (double)(sd * sd)));
-        float tx = (float)(x - (int32_t)(kernelSize / 2.0));
-        float ty = (float)(y - (int32_t)(kernelSize / 2.0));
-        float t2 = (float)(-(double)(tx * tx + ty * ty) / (2.0 * (double)sd * (double)sd));
-        kern[(size_t)(x + y * ks)] = t1 * std::exp(t2);
-      }
-  }
-  struct Buf {
-    std::vector<void*> p;
-    ~Buf() {
-      for (void* q : p) cudaFree(q);
+  return guarded("er_postprocess", [&]() -> er_status {
+    if (!rgba_in || width <= 0 || height <= 0 || (!rgba_out && !ldr_out))
+      return fail(ER_ERR_INVALID_ARG, "bad post-processing arguments");
+    if ((int64_t)width * height > ((int64_t)1 << 28)) return fail(ER_ERR_INVALID_ARG, "image too large");
+    er_post_opts o{};
+    o.exposure = 1.0f;
+    if (opts) o = *opts;
+    if (o.tonemap < ER_TONEMAP_NONE || o.tonemap > ER_TONEMAP_ACES) return fail(ER_ERR_INVALID_ARG, "tonemap");
+    if (o.bloom_power != 0.0f && !(o.bloom_radius >= 0.0f && o.bloom_radius <= 256.0f))
+      return fail(ER_ERR_INVALID_ARG, "bloom radius out of range");
+    int dev = 0;
+    ER_CUDA(cudaGetDevice(&dev));
+    const bool devp = flags & ER_RENDER_DEVICE_OUT;
+    const size_t n = (size_t)width * height;
+    PostParams P;
+    P.w = width;
+    P.h = height;
+    P.exposure = o.exposure;
+    P.tonemap = o.tonemap;
+    P.clamp01 = o.clamp != 0;
+    P.srgb = o.srgb != 0;
+    P.flip_x = o.flip_x != 0;
+    P.flip_y = o.flip_y != 0;
+    P.threshold = o.bloom_threshold;
+    P.power = o.bloom_power;
+    P.blur = o.bloom_power != 0.0f ? (int32_t)(o.bloom_radius / 2) : 0;
+    // basicBlur's kernel (PostProcessing.cpp:144-152), built on the host
+    const int32_t ks = 2 * P.blur + 1;
+    std::vector<float> kern(P.blur > 0 ? (size_t)ks * ks : 1, 0.0f);
+    if (P.blur > 0) {
+      const float sd = o.bloom_radius;
+      const float kernelSize = (float)ks;
+      for (int32_t x = 0; x < ks; x++)
+        for (int32_t y = 0; y < ks; y++) {
+          float t1 = (float)(1.0 / ((2.0 * (double)3.14159265358979323846f) * (double)(sd * sd)));
+          float tx = (float)(x - (int32_t)(kernelSize / 2.0));
+          float ty = (float)(y - (int32_t)(kernelSize / 2.0));
+          float t2 = (float)(-(double)(tx * tx + ty * ty) / (2.0 * (double)sd * (double)sd));
+          kern[(size_t)(x + y * ks)] = t1 * std::exp(t2);
+        }
     }
-    er_status get(void** out, size_t bytes) {
-      cudaError_t e = cudaMalloc(out, std::max<size_t>(bytes, 16));
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(ER_ERR_OOM, "post-processing buffers");
+    struct Buf {
+      std::vector<void*> p;
+      ~Buf() {
+        for (void* q : p) cudaFree(q);
       }
-      p.push_back(*out);
-      return ER_OK;
+      er_status get(void** out, size_t bytes) {
+        cudaError_t e = cudaMalloc(out, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          return fail(ER_ERR_OOM, "post-processing buffers");
+        }
+        p.push_back(*out);
+        return ER_OK;
+      }
+    } B;
+    er_status st;
+    const float4* d_in = (const float4*)rgba_in;
+    float4 *img, *thr = nullptr, *d_out = nullptr;
+    uchar4* d_ldr = nullptr;
+    float* d_kern = nullptr;
+    if (!devp) {
+      void* p;
+      if ((st = B.get(&p, n * 16)) != ER_OK) return st;
+      ER_CUDA(cudaMemcpy(p, rgba_in, n * 16, cudaMemcpyHostToDevice));
+      d_in = (const float4*)p;
     }
-  } B;
-  er_status st;
-  const float4* d_in = (const float4*)rgba_in;
-  float4 *img, *thr = nullptr, *d_out = nullptr;
-  uchar4* d_ldr = nullptr;
-  float* d_kern = nullptr;
-  if (!devp) {
-    void* p;
-    if ((st = B.get(&p, n * 16)) != ER_OK) return st;
-    ER_CUDA(cudaMemcpy(p, rgba_in, n * 16, cudaMemcpyHostToDevice));
-    d_in = (const float4*)p;
-  }
-  if ((st = B.get((void**)&img, n * 16)) != ER_OK) return st;
-  if (P.blur > 0) {
-    if ((st = B.get((void**)&thr, n * 16)) != ER_OK) return st;
-    if ((st = B.get((void**)&d_kern, kern.size() * 4)) != ER_OK) return st;
-    ER_CUDA(cudaMemcpy(d_kern, kern.data(), kern.size() * 4, cudaMemcpyHostToDevice));
-  }
-  if (rgba_out) {
-    if (devp) d_out = (float4*)rgba_out;
-    else if ((st = B.get((void**)&d_out, n * 16)) != ER_OK) return st;
-  }
-  if (ldr_out) {
-    if (devp) d_ldr = (uchar4*)ldr_out;
-    else if ((st = B.get((void**)&d_ldr, n * 4)) != ER_OK) return st;
-  }
-  const unsigned blocks = (unsigned)((n + 255) / 256);
-  k_post_pre<<<blocks, 256>>>(d_in, img, thr, P);
-  if (P.blur > 0) k_post_bloom<<<blocks, 256>>>(img, thr, d_kern, P);
-  k_post_finish<<<blocks, 256>>>(img, d_out, d_ldr, P);
-  ER_CUDA(cudaGetLastError());
-  if (!devp) {
-    if (rgba_out) ER_CUDA(cudaMemcpy(rgba_out, d_out, n * 16, cudaMemcpyDeviceToHost));
-    if (ldr_out) ER_CUDA(cudaMemcpy(ldr_out, d_ldr, n * 4, cudaMemcpyDeviceToHost));
-  }
-  ER_CUDA(cudaDeviceSynchronize());
-  (void)dev;
-  return ER_OK;
+    if ((st = B.get((void**)&img, n * 16)) != ER_OK) return st;
+    if (P.blur > 0) {
+      if ((st = B.get((void**)&thr, n * 16)) != ER_OK) return st;
+      if ((st = B.get((void**)&d_kern, kern.size() * 4)) != ER_OK) return st;
+      ER_CUDA(cudaMemcpy(d_kern, kern.data(), kern.size() * 4, cudaMemcpyHostToDevice));
+    }
+    if (rgba_out) {
+      if (devp) d_out = (float4*)rgba_out;
+      else if ((st = B.get((void**)&d_out, n * 16)) != ER_OK) return st;
+    }
+    if (ldr_out) {
+      if (devp) d_ldr = (uchar4*)ldr_out;
+      else if ((st = B.get((void**)&d_ldr, n * 4)) != ER_OK) return st;
+    }
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_post_pre<<<blocks, 256>>>(d_in, img, thr, P);
+    if (P.blur > 0) k_post_bloom<<<blocks, 256>>>(img, thr, d_kern, P);
+    k_post_finish<<<blocks, 256>>>(img, d_out, d_ldr, P);
+    ER_CUDA(cudaGetLastError());
+    if (!devp) {
+      if (rgba_out) ER_CUDA(cudaMemcpy(rgba_out, d_out, n * 16, cudaMemcpyDeviceToHost));
+      if (ldr_out) ER_CUDA(cudaMemcpy(ldr_out, d_ldr, n * 4, cudaMemcpyDeviceToHost));
+    }
+    ER_CUDA(cudaDeviceSynchronize());
+    (void)dev;
+    return ER_OK;
+  });
 }

@@ -1074,144 +1074,152 @@ using namespace er;
 
 extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, float* normal, float* tangent,
                                   float* bitangent, uint32_t* samples, uint32_t* pathcount) {
-  if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
-  Film& F = s->film;
-  if (!F.beauty) return fail(ER_ERR_INVALID_ARG, "nothing rendered yet");
-  bool dev = flags & ER_RENDER_DEVICE_OUT;
-  size_t np = (size_t)F.w * F.h;
-  er_status st;
-  if ((st = copy_out(s, dev, beauty, F.beauty, np * sizeof(float4))) != ER_OK) return st;
-  float* aovs[3] = {normal, tangent, bitangent};
-  for (int k = 0; k < 3; k++) {
-    if (!aovs[k]) continue;
-    if (!F.aov_on) return fail(ER_ERR_INVALID_ARG, "AOV passes were not rendered");
-    if ((st = copy_out(s, dev, aovs[k], F.aov[k], np * sizeof(float4))) != ER_OK) return st;
-  }
-  if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
-  if ((st = copy_out(s, dev, pathcount, F.pathcount, np * sizeof(uint32_t))) != ER_OK) return st;
-  ER_CUDA(cudaStreamSynchronize(s->stream));
-  return ER_OK;
+  return guarded("er_film_read", [&]() -> er_status {
+    if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+    Film& F = s->film;
+    if (!F.beauty) return fail(ER_ERR_INVALID_ARG, "nothing rendered yet");
+    bool dev = flags & ER_RENDER_DEVICE_OUT;
+    size_t np = (size_t)F.w * F.h;
+    er_status st;
+    if ((st = copy_out(s, dev, beauty, F.beauty, np * sizeof(float4))) != ER_OK) return st;
+    float* aovs[3] = {normal, tangent, bitangent};
+    for (int k = 0; k < 3; k++) {
+      if (!aovs[k]) continue;
+      if (!F.aov_on) return fail(ER_ERR_INVALID_ARG, "AOV passes were not rendered");
+      if ((st = copy_out(s, dev, aovs[k], F.aov[k], np * sizeof(float4))) != ER_OK) return st;
+    }
+    if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
+    if ((st = copy_out(s, dev, pathcount, F.pathcount, np * sizeof(uint32_t))) != ER_OK) return st;
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_snapshot(er_scene* s, float* beauty, uint32_t* samples) {
-  if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
-  ER_CUDA(cudaSetDevice(s->device));
-  std::lock_guard<std::mutex> lk(s->snap_mu);
-  if (!s->snap_valid) return fail(ER_ERR_INVALID_ARG, "no snapshot yet (render with ER_RENDER_SNAPSHOTS)");
-  const size_t np = (size_t)s->snap_w * s->snap_h;
-  ER_CUDA(cudaStreamWaitEvent(s->snap_stream, s->snap_event, 0));
-  if (beauty) ER_CUDA(cudaMemcpyAsync(beauty, s->snap_beauty, np * sizeof(float4), cudaMemcpyDeviceToHost, s->snap_stream));
-  if (samples) ER_CUDA(cudaMemcpyAsync(samples, s->snap_samples, np * 4, cudaMemcpyDeviceToHost, s->snap_stream));
-  ER_CUDA(cudaStreamSynchronize(s->snap_stream));
-  return ER_OK;
+  return guarded("er_snapshot", [&]() -> er_status {
+    if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+    ER_CUDA(cudaSetDevice(s->device));
+    std::lock_guard<std::mutex> lk(s->snap_mu);
+    if (!s->snap_valid) return fail(ER_ERR_INVALID_ARG, "no snapshot yet (render with ER_RENDER_SNAPSHOTS)");
+    const size_t np = (size_t)s->snap_w * s->snap_h;
+    ER_CUDA(cudaStreamWaitEvent(s->snap_stream, s->snap_event, 0));
+    if (beauty) ER_CUDA(cudaMemcpyAsync(beauty, s->snap_beauty, np * sizeof(float4), cudaMemcpyDeviceToHost, s->snap_stream));
+    if (samples) ER_CUDA(cudaMemcpyAsync(samples, s->snap_samples, np * 4, cudaMemcpyDeviceToHost, s->snap_stream));
+    ER_CUDA(cudaStreamSynchronize(s->snap_stream));
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beauty, float* normal, float* tangent,
                                float* bitangent, uint32_t* samples, uint32_t* pathcount, er_render_stats* stats) {
-  er_status st = check_opts(s, o);
-  if (st != ER_OK) return st;
-  const bool aov = o->flags & ER_RENDER_AOV;
-  const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
-  if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
-  if ((st = build_env_lut(s)) != ER_OK) return st;
-  if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
-  if ((o->flags & ER_RENDER_SNAPSHOTS) && (st = ensure_snapshot(s)) != ER_OK) return st;
-  const bool keep = o->flags & ER_RENDER_KEEP_PATHS;
-  s->kp_valid = false;
-  if (keep) {
-    const int64_t need = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
-    if (need > s->kp_cap) {
-      ER_CUDA(cudaStreamSynchronize(s->stream));
-      cudaFree(s->kp_rad);
-      s->kp_rad = nullptr;
-      s->kp_cap = 0;
-      if (cudaMalloc(&s->kp_rad, (size_t)std::max<int64_t>(need, 1) * 12) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(ER_ERR_OOM, "kept-path radiance allocation failed");
+  return guarded("er_render", [&]() -> er_status {
+    er_status st = check_opts(s, o);
+    if (st != ER_OK) return st;
+    const bool aov = o->flags & ER_RENDER_AOV;
+    const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
+    if ((o->flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) return st;
+    if ((st = build_env_lut(s)) != ER_OK) return st;
+    if ((st = ensure_film(s, aov, fp64, !(o->flags & ER_RENDER_CONTINUE))) != ER_OK) return st;
+    if ((o->flags & ER_RENDER_SNAPSHOTS) && (st = ensure_snapshot(s)) != ER_OK) return st;
+    const bool keep = o->flags & ER_RENDER_KEEP_PATHS;
+    s->kp_valid = false;
+    if (keep) {
+      const int64_t need = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
+      if (need > s->kp_cap) {
+        ER_CUDA(cudaStreamSynchronize(s->stream));
+        cudaFree(s->kp_rad);
+        s->kp_rad = nullptr;
+        s->kp_cap = 0;
+        if (cudaMalloc(&s->kp_rad, (size_t)std::max<int64_t>(need, 1) * 12) != cudaSuccess) {
+          cudaGetLastError();
+          return fail(ER_ERR_OOM, "kept-path radiance allocation failed");
+        }
+        s->kp_cap = need;
       }
-      s->kp_cap = need;
     }
-  }
-  unsigned long long st0[8];
-  ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
-  ER_CUDA(cudaEventRecord(s->ev0, s->stream));
-  int64_t launches = 0;
-  if ((st = run(s, o, nullptr, nullptr, &launches)) != ER_OK) return st;
-  if (keep) {
-    s->kp_valid = true;
-    s->kp_seed = o->seed;
-    s->kp_begin = o->sample_begin;
-    s->kp_spp = o->spp;
-    s->kp_depth = o->max_depth > 0 ? o->max_depth : 5;
-    s->kp_flags = o->flags & ER_RENDER_ENV_ALIAS;
-    s->kp_version = s->version;
-  }
-  ER_CUDA(cudaEventRecord(s->ev1, s->stream));
-  if (!(o->flags & ER_RENDER_NO_OUTPUT)) {
-    uint32_t fl = o->flags & ER_RENDER_DEVICE_OUT;
-    if ((st = er_film_read(s, fl, beauty, aov ? normal : nullptr, aov ? tangent : nullptr,
-                           aov ? bitangent : nullptr, samples, pathcount)) != ER_OK)
-      return st;
-  }
-  ER_CUDA(cudaEventSynchronize(s->ev1));
-  if ((st = check_device_error(s)) != ER_OK) return st;
-  if (stats) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-    unsigned long long st1[8];
-    ER_CUDA(cudaMemcpy(st1, s->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
-    std::memset(stats, 0, sizeof *stats);
-    stats->ms = ms;
-    stats->samples = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
-    stats->rays_closest = (int64_t)(st1[0] - st0[0]);
-    stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
-    stats->closest_nodes = (int64_t)(st1[2] - st0[2]);
-    stats->closest_tris = (int64_t)(st1[3] - st0[3]);
-    stats->shadow_nodes = (int64_t)(st1[4] - st0[4]);
-    stats->shadow_tris = (int64_t)(st1[5] - st0[5]);
-    stats->path_vertices = (int64_t)(st1[6] - st0[6]);
-    stats->kernel_launches = launches;
-    for (size_t k = 0; k < s->ev_stage.size(); k++) {
-      float e = 0;
-      cudaEventElapsedTime(&e, s->ev_pool[k], s->ev_pool[k + 1]);
-      stats->stage_ms[s->ev_stage[k]] += e;
-      stats->stage_launches[s->ev_stage[k]]++;
+    unsigned long long st0[8];
+    ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
+    ER_CUDA(cudaEventRecord(s->ev0, s->stream));
+    int64_t launches = 0;
+    if ((st = run(s, o, nullptr, nullptr, &launches)) != ER_OK) return st;
+    if (keep) {
+      s->kp_valid = true;
+      s->kp_seed = o->seed;
+      s->kp_begin = o->sample_begin;
+      s->kp_spp = o->spp;
+      s->kp_depth = o->max_depth > 0 ? o->max_depth : 5;
+      s->kp_flags = o->flags & ER_RENDER_ENV_ALIAS;
+      s->kp_version = s->version;
     }
-  }
-  return ER_OK;
+    ER_CUDA(cudaEventRecord(s->ev1, s->stream));
+    if (!(o->flags & ER_RENDER_NO_OUTPUT)) {
+      uint32_t fl = o->flags & ER_RENDER_DEVICE_OUT;
+      if ((st = er_film_read(s, fl, beauty, aov ? normal : nullptr, aov ? tangent : nullptr,
+                             aov ? bitangent : nullptr, samples, pathcount)) != ER_OK)
+        return st;
+    }
+    ER_CUDA(cudaEventSynchronize(s->ev1));
+    if ((st = check_device_error(s)) != ER_OK) return st;
+    if (stats) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+      unsigned long long st1[8];
+      ER_CUDA(cudaMemcpy(st1, s->d_stats, sizeof st1, cudaMemcpyDeviceToHost));
+      std::memset(stats, 0, sizeof *stats);
+      stats->ms = ms;
+      stats->samples = (int64_t)o->spp * s->camera.x_res * s->camera.y_res;
+      stats->rays_closest = (int64_t)(st1[0] - st0[0]);
+      stats->rays_shadow = (int64_t)(st1[1] - st0[1]);
+      stats->closest_nodes = (int64_t)(st1[2] - st0[2]);
+      stats->closest_tris = (int64_t)(st1[3] - st0[3]);
+      stats->shadow_nodes = (int64_t)(st1[4] - st0[4]);
+      stats->shadow_tris = (int64_t)(st1[5] - st0[5]);
+      stats->path_vertices = (int64_t)(st1[6] - st0[6]);
+      stats->kernel_launches = launches;
+      for (size_t k = 0; k < s->ev_stage.size(); k++) {
+        float e = 0;
+        cudaEventElapsedTime(&e, s->ev_pool[k], s->ev_pool[k + 1]);
+        stats->stage_ms[s->ev_stage[k]] += e;
+        stats->stage_launches[s->ev_stage[k]]++;
+      }
+    }
+    return ER_OK;
+  });
 }
 
 extern "C" er_status er_render_paths(er_scene* s, const er_render_opts* o, float* radiance, int32_t* bounces) {
-  er_status st = check_opts(s, o);
-  if (st != ER_OK) return st;
-  if (!radiance || !bounces) return fail(ER_ERR_INVALID_ARG, "NULL output");
-  size_t n = (size_t)o->spp * s->camera.x_res * s->camera.y_res;
-  if (n == 0) return ER_OK;
-  float* d_rad = nullptr;
-  int32_t* d_b = nullptr;
-  if (cudaMalloc(&d_rad, n * 3 * sizeof(float)) != cudaSuccess || cudaMalloc(&d_b, n * sizeof(int32_t)) != cudaSuccess) {
-    cudaGetLastError();
-    cudaFree(d_rad);
-    return fail(ER_ERR_OOM, "path dump allocation failed");
-  }
-  er_render_opts oo = *o;
-  oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
-  if (((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) || (st = build_env_lut(s)) != ER_OK) {
+  return guarded("er_render_paths", [&]() -> er_status {
+    er_status st = check_opts(s, o);
+    if (st != ER_OK) return st;
+    if (!radiance || !bounces) return fail(ER_ERR_INVALID_ARG, "NULL output");
+    size_t n = (size_t)o->spp * s->camera.x_res * s->camera.y_res;
+    if (n == 0) return ER_OK;
+    float* d_rad = nullptr;
+    int32_t* d_b = nullptr;
+    if (cudaMalloc(&d_rad, n * 3 * sizeof(float)) != cudaSuccess || cudaMalloc(&d_b, n * sizeof(int32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(d_rad);
+      return fail(ER_ERR_OOM, "path dump allocation failed");
+    }
+    er_render_opts oo = *o;
+    oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
+    if (((oo.flags & ER_RENDER_ENV_ALIAS) && (st = build_env_alias(s)) != ER_OK) || (st = build_env_lut(s)) != ER_OK) {
+      cudaFree(d_rad);
+      cudaFree(d_b);
+      return st;
+    }
+    st = run(s, &oo, d_rad, d_b, nullptr);
+    if (st == ER_OK) {
+      cudaMemcpyAsync(radiance, d_rad, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+      cudaMemcpyAsync(bounces, d_b, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+      cudaError_t e = cudaStreamSynchronize(s->stream);
+      if (e != cudaSuccess) st = cuda_fail(e, "er_render_paths");
+    }
     cudaFree(d_rad);
     cudaFree(d_b);
+    if (st == ER_OK) st = check_device_error(s);
     return st;
-  }
-  st = run(s, &oo, d_rad, d_b, nullptr);
-  if (st == ER_OK) {
-    cudaMemcpyAsync(radiance, d_rad, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
-    cudaMemcpyAsync(bounces, d_b, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
-    cudaError_t e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) st = cuda_fail(e, "er_render_paths");
-  }
-  cudaFree(d_rad);
-  cudaFree(d_b);
-  if (st == ER_OK) st = check_device_error(s);
-  return st;
+  });
 }
 
 // ------------------------------------------------------------------------
@@ -1304,60 +1312,62 @@ WaveView noalloc_view(unsigned char* base, unsigned long long*& stats) {
 
 extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, float* beauty, uint32_t* samples,
                                        uint32_t* pathcount) {
-  er_status st = check_opts(s, o);
-  if (st != ER_OK) return st;
-  if (!beauty || !samples || !pathcount) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: NULL film buffer");
-  if ((uintptr_t)beauty % 16 != 0) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: beauty must be 16-byte aligned");
-  const uint32_t allowed = ER_RENDER_CONTINUE;
-  if (o->flags & ~allowed)
-    return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: only ER_RENDER_CONTINUE is supported");
-  const int32_t W = s->camera.x_res, H = s->camera.y_res;
-  const int64_t npix = (int64_t)W * H;
-  if (npix > kNoAllocPaths)
-    return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: " + std::to_string(npix) + " pixels exceed the limit of " +
-                                        std::to_string(kNoAllocPaths) + " (ER_NOALLOC_MAX_PATHS)");
-  unsigned char* base = nullptr;
-  if ((st = noalloc_scratch(s->device, &base)) != ER_OK) return st;
-  unsigned long long* stats = nullptr;
-  WaveView w = noalloc_view(base, stats);
-  Film F;
-  F.w = W;
-  F.h = H;
-  F.beauty = (float4*)beauty;
-  F.samples = samples;
-  F.pathcount = pathcount;
-  F.aov_on = false;
-  if (!(o->flags & ER_RENDER_CONTINUE)) {
-    k_film_clear<<<(unsigned)((npix + 255) / 256), 256, 0, s->stream>>>(F, (int32_t)npix);
-  }
-  const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
-  int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : (int32_t)(kNoAllocPaths / npix);
-  sw = std::max(1, std::min(sw, (int32_t)(kNoAllocPaths / npix)));
-  WaveParams P;
-  P.W = W; P.H = H; P.npix = (int32_t)npix; P.max_depth = max_depth;
-  P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
-  P.flags = 0;
-  const int g_tr = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
-  const int g_tr8 = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
-  const int g_sh = grid_for(k_shade<false>, 128, s->num_sms);
-  const BatchView NB;
-  for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
-    int32_t cur = std::min(sw, o->spp - s0);
-    P.spp_wave = cur;
-    P.sample_base = o->sample_begin + s0;
-    int32_t n = cur * (int32_t)npix;
-    k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, GradArgs{});  // also zeroes the queue counters
-    for (int32_t b = 0; b <= max_depth; b++) {
-      if (s->dev.use_q8)
-        k_trace<true, false, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
-      else
-        k_trace<false, false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
-      if (b == max_depth) break;
-      k_shade<false><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB, GradArgs{});
+  return guarded("er_render_noalloc", [&]() -> er_status {
+    er_status st = check_opts(s, o);
+    if (st != ER_OK) return st;
+    if (!beauty || !samples || !pathcount) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: NULL film buffer");
+    if ((uintptr_t)beauty % 16 != 0) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: beauty must be 16-byte aligned");
+    const uint32_t allowed = ER_RENDER_CONTINUE;
+    if (o->flags & ~allowed)
+      return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: only ER_RENDER_CONTINUE is supported");
+    const int32_t W = s->camera.x_res, H = s->camera.y_res;
+    const int64_t npix = (int64_t)W * H;
+    if (npix > kNoAllocPaths)
+      return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: " + std::to_string(npix) + " pixels exceed the limit of " +
+                                          std::to_string(kNoAllocPaths) + " (ER_NOALLOC_MAX_PATHS)");
+    unsigned char* base = nullptr;
+    if ((st = noalloc_scratch(s->device, &base)) != ER_OK) return st;
+    unsigned long long* stats = nullptr;
+    WaveView w = noalloc_view(base, stats);
+    Film F;
+    F.w = W;
+    F.h = H;
+    F.beauty = (float4*)beauty;
+    F.samples = samples;
+    F.pathcount = pathcount;
+    F.aov_on = false;
+    if (!(o->flags & ER_RENDER_CONTINUE)) {
+      k_film_clear<<<(unsigned)((npix + 255) / 256), 256, 0, s->stream>>>(F, (int32_t)npix);
     }
-    k_accumulate<false><<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur, NB);
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "er_render_noalloc launch");
-  return check_device_error(s);
+    const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
+    int32_t sw = o->spp_per_wave > 0 ? o->spp_per_wave : (int32_t)(kNoAllocPaths / npix);
+    sw = std::max(1, std::min(sw, (int32_t)(kNoAllocPaths / npix)));
+    WaveParams P;
+    P.W = W; P.H = H; P.npix = (int32_t)npix; P.max_depth = max_depth;
+    P.k0 = (uint32_t)o->seed; P.k1 = (uint32_t)(o->seed >> 32);
+    P.flags = 0;
+    const int g_tr = grid_for(k_trace<false, false, false>, kTravBlock, s->num_sms);
+    const int g_tr8 = grid_for(k_trace<true, false, false>, kTravBlock, s->num_sms);
+    const int g_sh = grid_for(k_shade<false>, 128, s->num_sms);
+    const BatchView NB;
+    for (int32_t s0 = 0; s0 < o->spp; s0 += sw) {
+      int32_t cur = std::min(sw, o->spp - s0);
+      P.spp_wave = cur;
+      P.sample_base = o->sample_begin + s0;
+      int32_t n = cur * (int32_t)npix;
+      k_raygen<false><<<(n + 255) / 256, 256, 0, s->stream>>>(s->dev, w, P, n, NB, GradArgs{});  // also zeroes the queue counters
+      for (int32_t b = 0; b <= max_depth; b++) {
+        if (s->dev.use_q8)
+          k_trace<true, false, false><<<g_tr8, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+        else
+          k_trace<false, false, false><<<g_tr, kTravBlock, 0, s->stream>>>(s->dev, w, b, s->err_word, NB, 7u);
+        if (b == max_depth) break;
+        k_shade<false><<<g_sh, 128, 0, s->stream>>>(s->dev, w, P, b, NB, GradArgs{});
+      }
+      k_accumulate<false><<<(unsigned)((npix + 127) / 128), 128, 0, s->stream>>>(w, P, F, cur, NB);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "er_render_noalloc launch");
+    return check_device_error(s);
+  });
 }

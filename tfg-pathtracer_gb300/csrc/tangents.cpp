@@ -118,8 +118,10 @@ void compute_tangents(int64_t n_tris, const float* pos, const float* nrm_in, con
 
 extern "C" er_status er_compute_tangents(int64_t tri_count, const float* positions, const float* normals,
                                          const float* uvs, float* tangents, float* tangent_sign) {
-  if (tri_count < 0 || (tri_count > 0 && (!positions || !normals || !uvs || !tangents || !tangent_sign)))
-    return er::fail(ER_ERR_INVALID_ARG, "bad tangent arguments");
-  er::compute_tangents(tri_count, positions, normals, uvs, tangents, tangent_sign);
-  return ER_OK;
+  return er::guarded("er_compute_tangents", [&]() -> er_status {
+    if (tri_count < 0 || (tri_count > 0 && (!positions || !normals || !uvs || !tangents || !tangent_sign)))
+      return er::fail(ER_ERR_INVALID_ARG, "bad tangent arguments");
+    er::compute_tangents(tri_count, positions, normals, uvs, tangents, tangent_sign);
+    return ER_OK;
+  });
 }

@@ -55,75 +55,77 @@ using namespace er;
 
 extern "C" er_status er_trace_closest(er_scene* s, const float* rays, int64_t n, int32_t* tri_id, float* dist,
                                       float* uv, uint32_t flags, er_trace_stats* stats) {
-  if (!s || n < 0 || (n > 0 && (!rays || !tri_id))) return fail(ER_ERR_INVALID_ARG, "bad argument");
-  if (n > 0x7FFFFFFF) return fail(ER_ERR_INVALID_ARG, "more than 2^31-1 rays in one call");
-  ER_CUDA(cudaSetDevice(s->device));
-  if (n == 0) return ER_OK;
-  const bool dev = flags & ER_TRACE_DEVICE_PTRS;
-  const bool want_stats = (flags & ER_TRACE_STATS) && stats;
-  const float* d_rays = rays;
-  int32_t* d_tri = tri_id;
-  float *d_dist = dist, *d_uv = uv;
-  std::vector<void*> tmp;
-  auto cleanup = [&]() {
-    for (void* p : tmp) cudaFree(p);
-  };
-  if (!dev) {
-    void *a = nullptr, *b = nullptr, *c = nullptr, *e = nullptr;
-    if (cudaMalloc(&a, (size_t)n * 6 * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&b, (size_t)n * sizeof(int32_t)) != cudaSuccess ||
-        (dist && cudaMalloc(&c, (size_t)n * sizeof(float)) != cudaSuccess) ||
-        (uv && cudaMalloc(&e, (size_t)n * 2 * sizeof(float)) != cudaSuccess)) {
-      cudaGetLastError();
-      cudaFree(a); cudaFree(b); cudaFree(c); cudaFree(e);
-      return fail(ER_ERR_OOM, "trace buffers");
+  return guarded("er_trace_closest", [&]() -> er_status {
+    if (!s || n < 0 || (n > 0 && (!rays || !tri_id))) return fail(ER_ERR_INVALID_ARG, "bad argument");
+    if (n > 0x7FFFFFFF) return fail(ER_ERR_INVALID_ARG, "more than 2^31-1 rays in one call");
+    ER_CUDA(cudaSetDevice(s->device));
+    if (n == 0) return ER_OK;
+    const bool dev = flags & ER_TRACE_DEVICE_PTRS;
+    const bool want_stats = (flags & ER_TRACE_STATS) && stats;
+    const float* d_rays = rays;
+    int32_t* d_tri = tri_id;
+    float *d_dist = dist, *d_uv = uv;
+    std::vector<void*> tmp;
+    auto cleanup = [&]() {
+      for (void* p : tmp) cudaFree(p);
+    };
+    if (!dev) {
+      void *a = nullptr, *b = nullptr, *c = nullptr, *e = nullptr;
+      if (cudaMalloc(&a, (size_t)n * 6 * sizeof(float)) != cudaSuccess ||
+          cudaMalloc(&b, (size_t)n * sizeof(int32_t)) != cudaSuccess ||
+          (dist && cudaMalloc(&c, (size_t)n * sizeof(float)) != cudaSuccess) ||
+          (uv && cudaMalloc(&e, (size_t)n * 2 * sizeof(float)) != cudaSuccess)) {
+        cudaGetLastError();
+        cudaFree(a); cudaFree(b); cudaFree(c); cudaFree(e);
+        return fail(ER_ERR_OOM, "trace buffers");
+      }
+      tmp = {a, b, c, e};
+      d_rays = (const float*)a;
+      d_tri = (int32_t*)b;
+      d_dist = (float*)c;
+      d_uv = (float*)e;
+      cudaMemcpyAsync(a, rays, (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice, s->stream);
     }
-    tmp = {a, b, c, e};
-    d_rays = (const float*)a;
-    d_tri = (int32_t*)b;
-    d_dist = (float*)c;
-    d_uv = (float*)e;
-    cudaMemcpyAsync(a, rays, (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice, s->stream);
-  }
-  unsigned long long s0[16] = {0};
-  if (want_stats) cudaMemcpyAsync(s0, s->d_stats, sizeof s0, cudaMemcpyDeviceToHost, s->stream);
-  cudaEventRecord(s->ev0, s->stream);
-  int norm = (flags & ER_TRACE_NORMALIZED) ? 0 : 1;
-  if (s->dev.use_q8) {
-    if (want_stats) launch<true, true>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
-    else launch<true, false>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
-  } else {
-    if (want_stats) launch<false, true>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
-    else launch<false, false>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
-  }
-  cudaEventRecord(s->ev1, s->stream);
-  cudaError_t ce = cudaGetLastError();
-  if (ce != cudaSuccess) {
+    unsigned long long s0[16] = {0};
+    if (want_stats) cudaMemcpyAsync(s0, s->d_stats, sizeof s0, cudaMemcpyDeviceToHost, s->stream);
+    cudaEventRecord(s->ev0, s->stream);
+    int norm = (flags & ER_TRACE_NORMALIZED) ? 0 : 1;
+    if (s->dev.use_q8) {
+      if (want_stats) launch<true, true>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
+      else launch<true, false>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
+    } else {
+      if (want_stats) launch<false, true>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
+      else launch<false, false>(s, d_rays, n, norm, d_tri, d_dist, d_uv);
+    }
+    cudaEventRecord(s->ev1, s->stream);
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+      cleanup();
+      return cuda_fail(ce, "k_trace_rays launch");
+    }
+    if (!dev) {
+      cudaMemcpyAsync(tri_id, d_tri, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+      if (dist) cudaMemcpyAsync(dist, d_dist, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+      if (uv) cudaMemcpyAsync(uv, d_uv, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+    }
+    ce = cudaStreamSynchronize(s->stream);
     cleanup();
-    return cuda_fail(ce, "k_trace_rays launch");
-  }
-  if (!dev) {
-    cudaMemcpyAsync(tri_id, d_tri, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
-    if (dist) cudaMemcpyAsync(dist, d_dist, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
-    if (uv) cudaMemcpyAsync(uv, d_uv, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
-  }
-  ce = cudaStreamSynchronize(s->stream);
-  cleanup();
-  if (ce != cudaSuccess) return cuda_fail(ce, "er_trace_closest");
-  er_status st = check_device_error(s);
-  if (st != ER_OK) return st;
-  if (stats) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-    stats->ms = ms;
-    stats->node_visits = stats->box_tests = stats->tri_tests = 0;
-    if (want_stats) {
-      unsigned long long s1[16];
-      cudaMemcpy(s1, s->d_stats, sizeof s1, cudaMemcpyDeviceToHost);
-      stats->node_visits = (int64_t)(s1[8] - s0[8]);
-      stats->box_tests = (int64_t)(s1[9] - s0[9]);
-      stats->tri_tests = (int64_t)(s1[10] - s0[10]);
+    if (ce != cudaSuccess) return cuda_fail(ce, "er_trace_closest");
+    er_status st = check_device_error(s);
+    if (st != ER_OK) return st;
+    if (stats) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+      stats->ms = ms;
+      stats->node_visits = stats->box_tests = stats->tri_tests = 0;
+      if (want_stats) {
+        unsigned long long s1[16];
+        cudaMemcpy(s1, s->d_stats, sizeof s1, cudaMemcpyDeviceToHost);
+        stats->node_visits = (int64_t)(s1[8] - s0[8]);
+        stats->box_tests = (int64_t)(s1[9] - s0[9]);
+        stats->tri_tests = (int64_t)(s1[10] - s0[10]);
+      }
     }
-  }
-  return ER_OK;
+    return ER_OK;
+  });
 }
