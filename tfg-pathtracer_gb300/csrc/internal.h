@@ -297,6 +297,9 @@ struct er_scene {
   // launches fill the other's traversal tails
   er::Wave* wave2 = nullptr;
   cudaStream_t stream2 = nullptr;
+  // page-locked words read back by every render call without a blocking
+  // copy: the device error word at 0, the statistics counters at 64
+  unsigned char* h_pin = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_acc[2] = {nullptr, nullptr};
   uint32_t* err_word = nullptr;   // device error word (bounds / timeout)
   unsigned long long* d_stats = nullptr;  // device ray counters

@@ -1072,24 +1072,37 @@ er_status batch_launch(const DevScene& S, Wave* wv, const BatchSeg* d_segs, cons
 
 using namespace er;
 
+namespace er {
+namespace {
+
+// Queues the film copies on the scene's stream (the caller synchronises).
+er_status film_read_async(er_scene* s, uint32_t flags, float* beauty, float* normal, float* tangent,
+                          float* bitangent, uint32_t* samples, uint32_t* pathcount) {
+  Film& F = s->film;
+  if (!F.beauty) return fail(ER_ERR_INVALID_ARG, "nothing rendered yet");
+  bool dev = flags & ER_RENDER_DEVICE_OUT;
+  size_t np = (size_t)F.w * F.h;
+  er_status st;
+  if ((st = copy_out(s, dev, beauty, F.beauty, np * sizeof(float4))) != ER_OK) return st;
+  float* aovs[3] = {normal, tangent, bitangent};
+  for (int k = 0; k < 3; k++) {
+    if (!aovs[k]) continue;
+    if (!F.aov_on) return fail(ER_ERR_INVALID_ARG, "AOV passes were not rendered");
+    if ((st = copy_out(s, dev, aovs[k], F.aov[k], np * sizeof(float4))) != ER_OK) return st;
+  }
+  if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
+  return copy_out(s, dev, pathcount, F.pathcount, np * sizeof(uint32_t));
+}
+
+}  // namespace
+}  // namespace er
+
 extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, float* normal, float* tangent,
                                   float* bitangent, uint32_t* samples, uint32_t* pathcount) {
   return guarded("er_film_read", [&]() -> er_status {
     if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
-    Film& F = s->film;
-    if (!F.beauty) return fail(ER_ERR_INVALID_ARG, "nothing rendered yet");
-    bool dev = flags & ER_RENDER_DEVICE_OUT;
-    size_t np = (size_t)F.w * F.h;
-    er_status st;
-    if ((st = copy_out(s, dev, beauty, F.beauty, np * sizeof(float4))) != ER_OK) return st;
-    float* aovs[3] = {normal, tangent, bitangent};
-    for (int k = 0; k < 3; k++) {
-      if (!aovs[k]) continue;
-      if (!F.aov_on) return fail(ER_ERR_INVALID_ARG, "AOV passes were not rendered");
-      if ((st = copy_out(s, dev, aovs[k], F.aov[k], np * sizeof(float4))) != ER_OK) return st;
-    }
-    if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
-    if ((st = copy_out(s, dev, pathcount, F.pathcount, np * sizeof(uint32_t))) != ER_OK) return st;
+    er_status st = film_read_async(s, flags, beauty, normal, tangent, bitangent, samples, pathcount);
+    if (st != ER_OK) return st;
     ER_CUDA(cudaStreamSynchronize(s->stream));
     return ER_OK;
   });
@@ -1137,8 +1150,9 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
         s->kp_cap = need;
       }
     }
-    unsigned long long st0[8];
-    ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, sizeof st0, cudaMemcpyDeviceToHost, s->stream));
+    // counters before the call, into page-locked memory (no blocking copy)
+    unsigned long long* st0 = (unsigned long long*)(s->h_pin + 64);
+    if (stats) ER_CUDA(cudaMemcpyAsync(st0, s->d_stats, 64, cudaMemcpyDeviceToHost, s->stream));
     ER_CUDA(cudaEventRecord(s->ev0, s->stream));
     int64_t launches = 0;
     if ((st = run(s, o, nullptr, nullptr, &launches)) != ER_OK) return st;
@@ -1154,12 +1168,16 @@ extern "C" er_status er_render(er_scene* s, const er_render_opts* o, float* beau
     ER_CUDA(cudaEventRecord(s->ev1, s->stream));
     if (!(o->flags & ER_RENDER_NO_OUTPUT)) {
       uint32_t fl = o->flags & ER_RENDER_DEVICE_OUT;
-      if ((st = er_film_read(s, fl, beauty, aov ? normal : nullptr, aov ? tangent : nullptr,
-                             aov ? bitangent : nullptr, samples, pathcount)) != ER_OK)
+      if ((st = film_read_async(s, fl, beauty, aov ? normal : nullptr, aov ? tangent : nullptr,
+                                aov ? bitangent : nullptr, samples, pathcount)) != ER_OK)
         return st;
     }
-    ER_CUDA(cudaEventSynchronize(s->ev1));
-    if ((st = check_device_error(s)) != ER_OK) return st;
+    // the device error word rides on the same stream: one wait for the
+    // film, the word and the call's end
+    uint32_t* h_err = (uint32_t*)s->h_pin;
+    ER_CUDA(cudaMemcpyAsync(h_err, s->err_word, 4, cudaMemcpyDeviceToHost, s->stream));
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    if (*h_err != 0 && (st = check_device_error(s)) != ER_OK) return st;
     if (stats) {
       float ms = 0;
       cudaEventElapsedTime(&ms, s->ev0, s->ev1);

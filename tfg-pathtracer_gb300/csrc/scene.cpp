@@ -226,6 +226,8 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
     }
     cudaEventCreate(&s->ev0);
     cudaEventCreate(&s->ev1);
+    ce = cudaHostAlloc((void**)&s->h_pin, 128, cudaHostAllocDefault);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaHostAlloc"));
 
     // ---- BVH
     const bool gpu_build = o.builder == ER_BUILDER_GPU;
@@ -455,6 +457,7 @@ extern "C" er_status er_scene_free(er_scene* s) {
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->h_pin) cudaFreeHost(s->h_pin);
     cudaFree(s->snap_beauty);
     cudaFree(s->snap_samples);
     if (s->snap_event) cudaEventDestroy(s->snap_event);
