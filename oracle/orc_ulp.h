@@ -10,7 +10,7 @@
  *   level 2  every call moved by one or two ulps.
  *
  * Math libraries for GPUs implement these functions with error bounds of a
- * few ulps, so comparing the plain oracle with this build measures how far
+ * few ulps, so comparing the plain oracle with liborc_ulp.so measures how far
  * the per-path results of a scene move under rounding differences of that
  * size alone (tests/test_oracle_sensitivity.py).  Nothing else changes.
  */
