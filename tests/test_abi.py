@@ -5,6 +5,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -127,6 +128,25 @@ def test_descriptor_checks_before_any_device_call():
         d.camera.focal_length = float("inf")
     rejected(inf_focal, b"camera parameter")
     assert L.er_scene_set_camera(None, None) == A.ER_ERR_INVALID_ARG
+
+
+def test_host_allocation_failure_is_a_status(tmp_path):
+    """A C++ exception does not cross the ABI: a PNG of 2^30 x 2^30 pixels
+    (the encoder reserves ~4.6 EB before reading a pixel) is ER_ERR_OOM.
+    Run in a child process, so that an escaped exception shows as its exit
+    status instead of ending the test run."""
+    code = ("import ctypes as C, sys\n"
+            f"sys.path.insert(0, {os.path.join(ROOT, 'tfg-pathtracer_gb300')!r})\n"
+            "from eleven import _lib\n"
+            "L = _lib.load()\n"
+            "px = (C.c_uint8 * 4)()\n"
+            f"st = L.er_write_image({str(tmp_path / 'big.png').encode()!r}, px, 1 << 30, 1 << 30, 0)\n"
+            "print(st, L.er_last_error().decode())\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    st, msg = r.stdout.strip().split(" ", 1)
+    assert int(st) == A.ER_ERR_OOM and "er_write_image" in msg, r.stdout
+    assert not (tmp_path / "big.png").exists()
 
 
 def test_no_device_is_reported_not_faked():
