@@ -147,6 +147,11 @@ def test_host_allocation_failure_is_a_status(tmp_path):
     st, msg = r.stdout.strip().split(" ", 1)
     assert int(st) == A.ER_ERR_OOM and "er_write_image" in msg, r.stdout
     assert not (tmp_path / "big.png").exists()
+    # a BMP's sizes are 32-bit: 70000 x 70000 is refused before any pixel is read
+    L = _lib.load()
+    px = (C.c_uint8 * 4)()
+    assert L.er_write_image(str(tmp_path / "big.bmp").encode(), px, 70000, 70000, 1) == A.ER_ERR_INVALID_ARG
+    assert b"BMP" in L.er_last_error()
 
 
 def test_no_device_is_reported_not_faked():

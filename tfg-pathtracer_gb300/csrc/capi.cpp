@@ -97,7 +97,11 @@ std::vector<uint8_t> encode_png(const uint8_t* rgba, int32_t w, int32_t h) {
   be32(ihdr, (uint32_t)w); be32(ihdr, (uint32_t)h);
   ihdr.push_back(8); ihdr.push_back(6); ihdr.push_back(0); ihdr.push_back(0); ihdr.push_back(0);
   chunk(out, "IHDR", ihdr);
-  chunk(out, "IDAT", z);
+  // a chunk length is 31 bits: the zlib stream goes into consecutive IDAT
+  // chunks of at most 1 GiB
+  const size_t kChunk = (size_t)1 << 30;
+  for (size_t p = 0; p < z.size(); p += kChunk)
+    chunk(out, "IDAT", std::vector<uint8_t>(z.begin() + p, z.begin() + std::min(z.size(), p + kChunk)));
   chunk(out, "IEND", {});
   return out;
 }
@@ -112,6 +116,7 @@ void le32(std::vector<uint8_t>& v, uint32_t x) {
 std::vector<uint8_t> encode_bmp(const uint8_t* rgba, int32_t w, int32_t h) {
   size_t stride = ((size_t)w * 3 + 3) & ~(size_t)3;
   std::vector<uint8_t> out;
+  out.reserve(54 + stride * h);
   out.push_back('B'); out.push_back('M');
   le32(out, (uint32_t)(54 + stride * h)); le32(out, 0); le32(out, 54);
   le32(out, 40); le32(out, (uint32_t)w); le32(out, (uint32_t)h);
@@ -173,6 +178,8 @@ extern "C" er_status er_write_image(const char* path, const uint8_t* rgba, int32
                                     int32_t as_bmp) {
   return guarded("er_write_image", [&]() -> er_status {
     if (!path || !rgba || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARG, "bad image arguments");
+    if (as_bmp && 54 + (((uint64_t)width * 3 + 3) & ~(uint64_t)3) * (uint64_t)height > 0xFFFFFFFFull)
+      return fail(ER_ERR_INVALID_ARG, "image too large for a BMP file (32-bit sizes)");
     std::vector<uint8_t> bytes = as_bmp ? encode_bmp(rgba, width, height) : encode_png(rgba, width, height);
     FILE* f = std::fopen(path, "wb");
     if (!f) return fail(ER_ERR_IO, std::string("cannot open ") + path);
