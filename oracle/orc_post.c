@@ -1,8 +1,8 @@
 /*
  * ORACLE - test infrastructure only.  Restatement of the reference's
- * PostProcessing.cpp functions (applyExposure :3-6, flipX / flipY :8-30,
- * clampPixels :32-35, reinhardTonemap :37-41, acesTonemap :43-55,
- * applysRGB :57-60, basicBlur :133-210) in the order the product's
+ * PostProcessing.cpp functions (applyExposure :3-6, flipX :19-28 / flipY :8-17,
+ * clampPixels :30-33, reinhardTonemap :35-39, acesTonemap :41-52,
+ * applysRGB :54-57, basicBlur :132-211) in the order the product's
  * er_postprocess applies them, with the reference's literal types (double
  * where its expressions hold a double literal).  basicBlur's uninitialised
  * reads (the alpha of below-threshold pixels, the blur of border pixels)

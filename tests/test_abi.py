@@ -99,6 +99,23 @@ def test_invalid_arguments_rejected():
     assert L.er_render(None, None, None, None, None, None, None, None, None) == 1
 
 
+def test_render_options_checked_before_the_scene():
+    """Options are validated before the scene handle is touched: the last
+    sample index sample_begin + spp - 1 must fit the device's int32 sample
+    counter (a large sample_begin, as sharded runs pass it, would otherwise
+    wrap and repeat random streams)."""
+    L = _lib.load()
+    o = A.er_render_opts(4, 2**31 - 2, 4, 0, 0, 0, 0)
+    for call in (lambda: L.er_render(None, C.byref(o), None, None, None, None, None, None, None),
+                 lambda: L.er_render_noalloc(None, C.byref(o), None, None, None),
+                 lambda: L.er_render_paths(None, C.byref(o), None, None)):
+        assert call() == A.ER_ERR_INVALID_ARG
+        assert b"INT32_MAX" in L.er_last_error()
+    o.sample_begin = 2**31 - 5  # the last sample index is INT32_MAX - 1: accepted, then the NULL scene
+    assert L.er_render(None, C.byref(o), None, None, None, None, None, None, None) == A.ER_ERR_INVALID_ARG
+    assert b"NULL" in L.er_last_error()
+
+
 def test_descriptor_checks_before_any_device_call():
     """NULL arrays with positive counts and non-finite camera fields are
     rejected as invalid arguments (no device is touched first)."""

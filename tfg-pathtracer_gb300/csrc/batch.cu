@@ -525,7 +525,8 @@ extern "C" er_status er_batch_set_jobs(er_batch* b, const er_batch_job* jobs, in
       if (J.scene < 0 || J.scene >= (int32_t)b->scenes.size()) return fail(ER_ERR_INVALID_ARG, "job scene out of range");
       er_status cs = validate_camera(J.camera);
       if (cs != ER_OK) return fail(cs, "job " + std::to_string(j) + ": " + er_last_error());
-      if (J.spp < 0 || J.sample_begin < 0 || J.max_depth < 0 || J.max_depth > 64)
+      if (J.spp < 0 || J.sample_begin < 0 || J.max_depth < 0 || J.max_depth > 64 ||
+          (int64_t)J.sample_begin + J.spp > INT32_MAX)
         return fail(ER_ERR_INVALID_ARG, "job options out of range");
       if (J.flags & ~(uint32_t)(ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64))
         return fail(ER_ERR_INVALID_ARG, "job flags: only ER_RENDER_ENV_ALIAS and ER_RENDER_ACCUM_FP64");

@@ -331,6 +331,9 @@ er_status upload(er_scene* s, void** p, const void* host, size_t bytes);
 DevCamera make_dev_camera(const er_camera& c);
 void free_wave(er_scene* s);
 void free_film(er_scene* s);
+// Looks up (again) the device address of er_render_noalloc's scratch array
+// on the current device, `device` (render.cu); errors are left to the call.
+void noalloc_prepare(int device);
 er_status check_device_error(er_scene* s);
 // Resolution (1 .. 2^28 pixels) and finite lens and pose parameters.
 er_status validate_camera(const er_camera& c);

@@ -1,7 +1,7 @@
 // Post-processing of a film on the GPU: the operations of the reference's
-// PostProcessing.cpp (applyExposure :3-6, basicBlur bloom :133-210,
-// reinhardTonemap :37-41, acesTonemap :43-55, clampPixels :32-35, applysRGB
-// :57-60, flipX / flipY :8-30) and its LDR output step (main.cpp:150-158:
+// PostProcessing.cpp (applyExposure :3-6, basicBlur bloom :132-211,
+// reinhardTonemap :35-39, acesTonemap :41-52, clampPixels :30-33, applysRGB
+// :54-57, flipX :19-28 / flipY :8-17) and its LDR output step (main.cpp:150-158:
 // clamp, fastPow(v, 1/2.2) * 255), one thread per pixel, in that order.
 // The arithmetic follows the reference's types: double where its
 // expressions hold a double literal (ACES, sRGB, the bloom threshold sum),
@@ -144,7 +144,7 @@ extern "C" er_status er_postprocess(const float* rgba_in, int32_t width, int32_t
     P.threshold = o.bloom_threshold;
     P.power = o.bloom_power;
     P.blur = o.bloom_power != 0.0f ? (int32_t)(o.bloom_radius / 2) : 0;
-    // basicBlur's kernel (PostProcessing.cpp:144-152), built on the host
+    // basicBlur's kernel (PostProcessing.cpp:143-153), built on the host
     const int32_t ks = 2 * P.blur + 1;
     std::vector<float> kern(P.blur > 0 ? (size_t)ks * ks : 1, 0.0f);
     if (P.blur > 0) {

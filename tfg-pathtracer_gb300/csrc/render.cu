@@ -881,9 +881,13 @@ er_status ensure_snapshot(er_scene* s) {
 }
 
 er_status check_opts(er_scene* s, const er_render_opts* o) {
-  if (!s || !o) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+  if (!o) return fail(ER_ERR_INVALID_ARG, "NULL argument");
   if (o->spp < 0 || o->sample_begin < 0 || o->max_depth < 0 || o->max_depth > 64 || o->spp_per_wave < 0)
     return fail(ER_ERR_INVALID_ARG, "render options out of range");
+  // sample indices are int32 on the device: the last one must fit
+  if ((int64_t)o->sample_begin + o->spp > INT32_MAX)
+    return fail(ER_ERR_INVALID_ARG, "sample_begin + spp exceeds INT32_MAX");
+  if (!s) return fail(ER_ERR_INVALID_ARG, "NULL argument");
   ER_CUDA(cudaSetDevice(s->device));
   return ER_OK;
 }
@@ -1280,18 +1284,25 @@ std::mutex g_noalloc_lock;
 unsigned char* g_noalloc_ptr[128];  // device address of the scratch, per device ordinal
 
 // Host code must not take the address of g_noalloc_scratch directly (that is
-// a host-side shadow); the device address is looked up once per device, with
-// that device current.
-er_status noalloc_scratch(int device, unsigned char** out) {
+// a host-side shadow); the device address is looked up with the device
+// current.  er_scene_create refreshes it (noalloc_prepare), so the lookup,
+// and with it the loading of this file's module that holds the array, happens
+// while a scene is being created and not inside er_render_noalloc; a scene
+// created after a cudaDeviceReset replaces the cached address of the old
+// context.
+er_status noalloc_lookup(int device, bool refresh, unsigned char** out) {
   std::lock_guard<std::mutex> lk(g_noalloc_lock);
   if (device < 0 || device >= 128) return fail(ER_ERR_INVALID_ARG, "device ordinal out of range");
-  if (!g_noalloc_ptr[device]) {
+  if (refresh || !g_noalloc_ptr[device]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
+    if (e != cudaSuccess || !p) {
+      g_noalloc_ptr[device] = nullptr;
+      return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
+    }
     g_noalloc_ptr[device] = (unsigned char*)p;
   }
-  *out = g_noalloc_ptr[device];
+  if (out) *out = g_noalloc_ptr[device];
   return ER_OK;
 }
 
@@ -1326,6 +1337,11 @@ WaveView noalloc_view(unsigned char* base, unsigned long long*& stats) {
 }
 
 }  // namespace
+
+void noalloc_prepare(int device) {
+  if (noalloc_lookup(device, true, nullptr) != ER_OK) cudaGetLastError();
+}
+
 }  // namespace er
 
 extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, float* beauty, uint32_t* samples,
@@ -1335,6 +1351,8 @@ extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, flo
     if (st != ER_OK) return st;
     if (!beauty || !samples || !pathcount) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: NULL film buffer");
     if ((uintptr_t)beauty % 16 != 0) return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: beauty must be 16-byte aligned");
+    if ((uintptr_t)samples % 4 != 0 || (uintptr_t)pathcount % 4 != 0)
+      return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: samples and pathcount must be 4-byte aligned");
     const uint32_t allowed = ER_RENDER_CONTINUE;
     if (o->flags & ~allowed)
       return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: only ER_RENDER_CONTINUE is supported");
@@ -1344,7 +1362,7 @@ extern "C" er_status er_render_noalloc(er_scene* s, const er_render_opts* o, flo
       return fail(ER_ERR_INVALID_ARG, "er_render_noalloc: " + std::to_string(npix) + " pixels exceed the limit of " +
                                           std::to_string(kNoAllocPaths) + " (ER_NOALLOC_MAX_PATHS)");
     unsigned char* base = nullptr;
-    if ((st = noalloc_scratch(s->device, &base)) != ER_OK) return st;
+    if ((st = noalloc_lookup(s->device, false, &base)) != ER_OK) return st;
     unsigned long long* stats = nullptr;
     WaveView w = noalloc_view(base, stats);
     Film F;

@@ -217,6 +217,9 @@ extern "C" er_status er_scene_create(const er_scene_desc* d, const er_scene_opts
     ce = cudaGetDeviceProperties(&prop, o.device);
     if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaGetDeviceProperties"));
     s->num_sms = prop.multiProcessorCount;
+    // er_render_noalloc's scratch address on this device (loads the module
+    // that holds the array now rather than in that allocation-free call)
+    noalloc_prepare(o.device);
     if (o.stream) {
       s->stream = (cudaStream_t)o.stream;
     } else {
