@@ -16,7 +16,10 @@ is inserted between steps.
 
 --impl reference times the reference's CPU path on the host cores: the
 oracle port of the reference (its depth-18 BVH, traversal and shading,
-restated in C), all host threads, a bounded pixel subset per step.
+restated in C), all host threads, a bounded pixel subset per step.  Its
+line also carries `reference_cuda`: the reference's own CUDA renderer
+(kernel.cu, built for sm_103a from the reference tree with four textual
+patches) timed on the GPU for this config and for the small scene.
 """
 from __future__ import annotations
 
@@ -54,6 +57,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="--impl reference: skip timing the reference's CUDA renderer on the GPU")
     ap.add_argument("--launch-rays", type=int, default=-1,
                     help="print the rays traced by trace launch B of a 1-spp wave (extension rays of bounce B "
                          "+ shadow rays of bounce B-1) and exit; used to turn an ncu capture of that launch "
@@ -218,6 +223,51 @@ def cpu_baseline(arrays, max_depth, seconds, seed=0):
                        f"{int(r['pathcount'].sum())} path vertices)"), dt
 
 
+REF_CUDA_PATCHES = [
+    "kernel.cu:156,158 `#if USEBVH:` / `#else:` without the colon (MSVC-only preprocessor syntax)",
+    "kernel.cu:781,783 std::sinf / std::cosf -> sinf / cosf (host debug printer; not in libstdc++'s std)",
+    "Definitions.h:9 MAXBOUNCES settable per build (4 for c0, 8 for c1)",
+    "kernel.cu:185 point-light index (int)(n * r1) clamped to n - 1 (cuRAND's uniform may return 1)",
+]
+
+
+def reference_cuda(arrays, max_depth, warm, spp):
+    """The reference's own CUDA renderer (kernel.cu renderingKernel, one
+    launch per sample) on this GPU through oracle/ref_cuda_main.cpp, built
+    from the reference tree by `make -C oracle refcuda` with the patches
+    above; CUDA events on the reference's kernelStream around renderCuda."""
+    from eleven.build import ORACLE, REF_SRC
+    if not os.path.isdir(REF_SRC):
+        return {"unavailable": "reference sources not present"}
+    t = time.perf_counter()
+    r = subprocess.run(["make", "-s", "-C", ORACLE, "-j4", "refcuda", "REF_DIR=" + REF_SRC], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        return {"unavailable": "reference CUDA build failed: " + (r.stdout + r.stderr)[-300:]}
+    build_s = time.perf_counter() - t
+    sys.path.insert(0, ORACLE)
+    import refcuda_scene
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "scene.ersc")
+        refcuda_scene.write(arrays, f)
+        exe = os.path.join(ORACLE, "_ref", f"ref_cuda_d{max_depth}")
+        if not os.path.exists(exe):
+            return {"unavailable": f"no reference build for depth {max_depth}"}
+        r = subprocess.run([exe, f, str(warm), str(spp)], capture_output=True, text=True, timeout=1200)
+    if r.returncode != 0:
+        return {"unavailable": f"reference CUDA run exited {r.returncode}: " + r.stdout[-200:] + r.stderr[-200:]}
+    res = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    W, H = res["width"], res["height"]
+    return {"value": round(W * H * spp / res["ms"] / 1e3, 3), "unit": UNIT, "ms": round(res["ms"], 2),
+            "spp": spp, "warmup_spp": warm, "resolution": f"{W}x{H}", "max_bounces": res["max_bounces"],
+            "kpaths_per_s": round(res["path_vertices"] / res["ms"], 1),
+            "render_setup_s": round(res["render_setup_ms"] / 1e3, 2), "build_s": round(build_s, 1),
+            "timing": "CUDA events on the reference's kernelStream around renderCuda (one renderingKernel "
+                      "launch and one stream synchronisation per sample, kernel.cu:665-686)",
+            "nvcc": "-O3 -use_fast_math -rdc=true -lineinfo, sm_103a (tfg-pathtracer.vcxproj:139-141)",
+            "patches": REF_CUDA_PATCHES}
+
+
 def run_reference(args):
     rank, world, local, pg = dist_setup(args.gpus)
     if rank != 0:
@@ -248,8 +298,16 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"per step 1 spp on every {stride}th pixel ({n} samples)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
     orc.close()
+    if not args.no_reference_cuda:
+        # the reference's CUDA renderer on this GPU: this config, and the
+        # small scene at its stated 16 spp x 4
+        rc = {args.config: reference_cuda(arrays, max_depth, 1, 4 if args.config == "c1" else 64)}
+        if args.config != "c0":
+            a0, d0, _ = make_scene("c0")
+            rc["c0"] = reference_cuda(a0, d0, 16, 64)
+        line["reference_cuda"] = rc
+    print(json.dumps(line), flush=True)
     return 0
 
 

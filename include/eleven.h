@@ -7,12 +7,12 @@
  *
  *   reference                                   replaced by
  *   cudaError_t renderSetup(Scene*)             er_scene_create / er_scene_load
- *     (kernel.h:81, kernel.cu:566-661)            (scene upload + BVH build)
+ *     (kernel.h:80, kernel.cu:566-661)            (scene upload + BVH build)
  *   cudaError_t renderCuda(Scene*, int spp)     er_render
- *     (kernel.h:79, kernel.cu:665-686)
+ *     (kernel.h:78, kernel.cu:665-686)
  *   cudaError_t getBuffers(RenderData&, int*,   er_render output buffers /
- *     int) (kernel.h:83, kernel.cu:688-710)       er_film_read
- *   int getSamples() (kernel.h:85,              er_film_read (samples array)
+ *     int) (kernel.h:82, kernel.cu:688-710)       er_film_read
+ *   int getSamples() (kernel.h:84,              er_film_read (samples array)
  *     kernel.cu:712-724)
  *   BVH::transverse (BVH.hpp:120-157) via      er_trace_closest (parity gate)
  *     throwRay (kernel.cu:152-173)
@@ -84,8 +84,9 @@ typedef struct er_material {
       transmission, specular, specular_tint, sheen_tint, subsurface, sheen;
 } er_material;
 
-/* Texture.hpp:196-214: float RGB texels, row-major, row 0 first as stored
- * after loading (loaders flip BMPs on load, Texture.hpp:230). */
+/* Texture.hpp:15-33 (data, width, height, xTile/yTile, xOffset/yOffset):
+ * float RGB texels, row-major, row 0 first as stored after loading (BMP
+ * textures are flipped vertically on load, Texture.hpp:49). */
 typedef struct er_texture {
   int32_t width, height;
   const float* data; /* width*height*3 */
@@ -168,6 +169,18 @@ er_status er_scene_create(const er_scene_desc* desc, const er_scene_opts* opts,
  * from scene.json. */
 er_status er_scene_load(const char* dir, const er_scene_opts* opts,
                         er_scene** out);
+/* The host half of er_scene_load, without a device: reads and parses a
+ * scene folder (SceneLoader.hpp:7-143 loadScene, ObjLoader.hpp:20-206,
+ * Texture.hpp:41-68, HDRI.hpp:42-60) into a description whose arrays the
+ * er_folder handle owns.  er_folder_desc copies that description (its
+ * pointers stay valid until er_folder_free); a caller may adjust it (the
+ * reference's harness sets Material fields its .mtl reader cannot express)
+ * and pass it to er_scene_create.  er_scene_load(dir) equals
+ * er_scene_create(desc of er_scene_folder_read(dir)). */
+typedef struct er_folder er_folder;
+er_status er_scene_folder_read(const char* dir, er_folder** out);
+er_status er_folder_desc(const er_folder* folder, er_scene_desc* out);
+er_status er_folder_free(er_folder* folder);
 er_status er_scene_info_get(const er_scene* scene, er_scene_info* out);
 /* Replace the camera of a built scene (no BVH rebuild). */
 er_status er_scene_set_camera(er_scene* scene, const er_camera* cam);
@@ -271,11 +284,19 @@ er_status er_snapshot(er_scene* scene, float* beauty, uint32_t* samples);
  * buffers: beauty W*H*4 floats (16-byte aligned), samples and pathcount
  * W*H uint32, laid out as in er_render.
  *  - W*H must not exceed ER_NOALLOC_MAX_PATHS (ER_ERR_INVALID_ARG otherwise);
- *    spp is traced in waves of floor(ER_NOALLOC_MAX_PATHS / (W*H)) samples.
+ *    spp is traced in waves of opts->spp_per_wave samples (0, or a larger
+ *    value: floor(ER_NOALLOC_MAX_PATHS / (W*H)) samples).
  *  - Only ER_RENDER_CONTINUE is accepted in opts->flags (FP32 running mean,
  *    no AOVs); without it the film is cleared first.
- *  - The first call on a device looks up the array's device address (with
- *    that device current); make that first call before any stream capture.
+ *  - beauty must be 16-byte aligned, samples and pathcount 4-byte aligned.
+ *  - The array's device address is looked up, with the scene's device
+ *    current, when a scene is created (er_scene_create / er_scene_load): under
+ *    CUDA's lazy module loading that is when the module holding the array is
+ *    loaded and its memory taken, so er_render_noalloc itself allocates
+ *    nothing.  If that lookup failed there, the first er_render_noalloc call
+ *    on the device repeats it; make that first call before any stream capture.
+ *    A cudaDeviceReset ends every scene of the device; the next scene created
+ *    there looks the address up again.
  *  - All calls share the array and it keeps the last call's contents (each
  *    wave re-initialises what it reads).  Calls whose work overlaps on the
  *    GPU (other streams, other threads) race on it: serialise them.
@@ -318,9 +339,9 @@ er_status er_compute_tangents(int64_t tri_count, const float* positions, const f
 
 /* ---------------------------------------------------------- post-process -- */
 /* The reference's PostProcessing.cpp as one GPU pass, applied in this
- * order: applyExposure (:3-6), basicBlur bloom (:133-210), Reinhard
- * (:37-41) or ACES (:43-55) tone map, clampPixels (:32-35), applysRGB
- * (:57-60), flipX / flipY (:8-30).  rgba_out receives the float result,
+ * order: applyExposure (:3-6), basicBlur bloom (:132-211), Reinhard
+ * (:35-39) or ACES (:41-52) tone map, clampPixels (:30-33), applysRGB
+ * (:54-57), flipX (:19-28) / flipY (:8-17).  rgba_out receives the float result,
  * ldr_out its 8-bit encoding as er_encode_ldr makes it (either may be
  * NULL).  flags: ER_RENDER_DEVICE_OUT for device pointers. */
 enum { ER_TONEMAP_NONE = 0, ER_TONEMAP_REINHARD = 1, ER_TONEMAP_ACES = 2 };
@@ -440,6 +461,18 @@ typedef struct er_trace_stats {
 er_status er_trace_closest(er_scene* scene, const float* rays, int64_t n,
                            int32_t* tri_id, float* dist, float* uv,
                            uint32_t flags, er_trace_stats* stats);
+
+/* ----------------------------------------------------------- measurement -- */
+/* Bandwidth ceilings of a GPU measured by this library's own streaming
+ * kernels (no counterpart in the reference; the denominators of the
+ * traversal and shading rooflines).  ER_BW_L2_READ: a buffer of `bytes`
+ * (1 MiB .. 64 MiB, resident in L2) read `reps` times with 16-byte loads
+ * cached in L2 only; ER_BW_HBM_COPY: a buffer of `bytes` (at least 1 MiB,
+ * at most 32 GiB; choose it far larger than L2) copied `reps` times, read +
+ * written bytes counted.  gbps = bytes moved / CUDA-event time.  Allocates
+ * and frees its buffers. */
+enum { ER_BW_L2_READ = 0, ER_BW_HBM_COPY = 1 };
+er_status er_device_bandwidth(int32_t device, int32_t kind, int64_t bytes, int32_t reps, double* gbps);
 
 /* ----------------------------------------------------------------- image -- */
 

@@ -65,3 +65,21 @@ def test_postprocess_rejects_bad_input():
         _lib.postprocess(img, W, H, tonemap=7)
     with pytest.raises(_lib.ElevenError):
         _lib.postprocess(img, 0, H)
+
+
+def test_postprocess_matches_reference_golden():
+    """er_postprocess against the reference's own PostProcessing.cpp
+    (golden outputs in tests/golden/reference_io.npz), on the pixels and
+    channels the reference defines; the sRGB power within 1 ulp."""
+    from test_loader_reference import GOLD, _post_cases
+    G = dict(np.load(GOLD))
+    n = 0
+    for k, w, h, o, px, ref, mask in _post_cases(G):
+        out, _ = _lib.postprocess(px, w, h, exposure=o.exposure, tonemap=o.tonemap, clamp=o.clamp, srgb=o.srgb,
+                                  flip_x=o.flip_x, flip_y=o.flip_y, bloom_threshold=o.bloom_threshold,
+                                  bloom_power=o.bloom_power, bloom_radius=o.bloom_radius)
+        a = out.view(np.uint32)[mask].astype(np.int64)
+        b = ref.view(np.uint32)[mask].astype(np.int64)
+        assert np.abs(a - b).max() <= (1 if o.srgb else 0), k
+        n += int(mask.sum())
+    assert n > 10_000

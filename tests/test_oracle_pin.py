@@ -89,3 +89,14 @@ def test_c0_bvh_and_traversal():
     assert np.array_equal(ia, ib) and same(da, db).all()
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_pins_hold_where_the_gpu_runs(libs):
+    """The same pins in the GPU session: there the reference headers and the
+    oracle are compiled for that machine's host CPU, so this checks that the
+    restatement still equals the reference built there."""
+    import inspect
+    for name, fn in list(globals().items()):
+        if name.startswith("test_") and name != "test_pins_hold_where_the_gpu_runs" and callable(fn):
+            fn(libs) if inspect.signature(fn).parameters else fn()

@@ -536,168 +536,216 @@ std::string join(const std::string& dir, const std::string& f) {
 }  // namespace
 }  // namespace er
 
+// A parsed scene folder: the description and the arrays it points into.
+struct er_folder {
+  er_scene_desc d{};
+  std::vector<float> env_data, pos, nrm, uv, tan, tsign;
+  std::vector<std::vector<float>> tex_data;
+  std::vector<er_texture> texs;
+  std::vector<er_material> mats;
+  std::vector<int32_t> tri_obj, obj_mat;
+  std::vector<er_point_light> lights;
+};
+
+namespace er {
+namespace {
+
+// The reference's loadScene (SceneLoader.hpp:7-143) into an er_folder.
+er_status read_folder(const std::string& dir, er_folder* F) {
+  std::string text;
+  if (!read_file(join(dir, "scene.json"), &text)) return fail(ER_ERR_IO, "cannot read " + join(dir, "scene.json"));
+  JVal root;
+  JParser jp(text);
+  if (!jp.val(&root) || root.kind != JVal::OBJ) return fail(ER_ERR_PARSE, "scene.json: malformed JSON");
+
+  er_scene_desc& d = F->d;
+  d = er_scene_desc{};
+  // camera (SceneLoader.hpp:25-46; Camera(xRes, yRes), Camera.hpp:29-37)
+  const JVal* cam = root.get("camera");
+  if (!cam) return fail(ER_ERR_PARSE, "scene.json: no camera");
+  double xr = 0, yr = 0, fl = 0, fd = 0, ap = 0;
+  if (!jnum(cam->get("xRes"), &xr) || !jnum(cam->get("yRes"), &yr))
+    return fail(ER_ERR_PARSE, "scene.json: camera needs xRes and yRes");
+  d.camera.x_res = (int32_t)xr;
+  d.camera.y_res = (int32_t)yr;
+  d.camera.sensor_width = (float)(35 * 0.001);
+  d.camera.sensor_height = d.camera.sensor_width * ((float)d.camera.y_res / (float)d.camera.x_res);
+  // a missing field reads as 0, as RSJresource::as<double>() returns its
+  // default argument, which overwrites Camera's own defaults
+  d.camera.focal_length = jnum(cam->get("focalLength"), &fl) ? (float)fl : 0.0f;
+  d.camera.focus_distance = jnum(cam->get("focusDistance"), &fd) ? (float)fd : 0.0f;
+  d.camera.aperture = jnum(cam->get("aperture"), &ap) ? (float)ap : 0.0f;
+  d.camera.bokeh = jbool(cam->get("bokeh")) ? 1 : 0;
+  if (!jvec3(cam->get("position"), d.camera.position)) std::memset(d.camera.position, 0, sizeof d.camera.position);
+  if (!jvec3(cam->get("rotation"), d.camera.rotation)) std::memset(d.camera.rotation, 0, sizeof d.camera.rotation);
+
+  // environment (SceneLoader.hpp:51-65, HDRI.hpp:22-60)
+  const JVal* hd = root.get("hdri");
+  if (!hd) return fail(ER_ERR_PARSE, "scene.json: no hdri");
+  int ew = 0, eh = 0;
+  if (const JVal* nm = hd->get("name")) {
+    std::string hp = join(join(dir, "HDRI"), nm->text + ".hdr");
+    std::string bytes;
+    if (!read_file(hp, &bytes)) return fail(ER_ERR_IO, "cannot read " + hp);
+    er_status st = decode_hdr(bytes, hp, &ew, &eh, &F->env_data);
+    if (st != ER_OK) return st;
+  } else if (const JVal* col = hd->get("color")) {
+    float c[3];
+    if (!jvec3(col, c)) return fail(ER_ERR_PARSE, "scene.json: hdri.color needs r, g, b");
+    ew = eh = 1024;
+    F->env_data.resize((size_t)ew * eh * 3);
+    for (size_t i = 0; i < (size_t)ew * eh; i++) {
+      F->env_data[3 * i] = c[0];
+      F->env_data[3 * i + 1] = c[1];
+      F->env_data[3 * i + 2] = c[2];
+    }
+  } else {
+    return fail(ER_ERR_PARSE, "scene.json: hdri needs name or color");
+  }
+  d.env.width = ew;
+  d.env.height = eh;
+  d.env.data = F->env_data.data();
+  d.env.x_tile = d.env.y_tile = 1.0f;
+  double off = 0;
+  if (jnum(hd->get("xOffset"), &off)) d.env.x_offset = (float)off;
+  if (jnum(hd->get("yOffset"), &off)) d.env.x_offset = (float)off;  // SceneLoader.hpp:64-65
+
+  // materials and textures (SceneLoader.hpp:67-107)
+  std::vector<Mtl> mtls;
+  if (read_file(join(dir, "scene.mtl"), &text)) {
+    er_status st = parse_mtl(text, &mtls);
+    if (st != ER_OK) return st;
+  }
+  std::vector<std::string> tex_paths;
+  for (Mtl& mt : mtls) {
+    for (auto& kv : mt.maps) {
+      const std::string& key = kv.first;
+      const std::string& mp = kv.second;
+      int id = (int)tex_paths.size();
+      bool dup = false;
+      for (size_t j = 0; j < tex_paths.size(); j++)
+        if (tex_paths[j] == mp) { id = (int)j; dup = true; }
+      float gamma = 1.0f;
+      if (key == "map_Kd") { mt.m.albedo_tex = id; gamma = 2.2f; }
+      if (key == "map_Ns") mt.m.roughness_tex = id;
+      if (key == "refl") mt.m.metallic_tex = id;
+      if (key == "map_Bump") mt.m.normal_tex = id;
+      if (dup) continue;
+      std::string p = file_exists(mp) ? mp : join(dir, mp);
+      std::string bytes;
+      if (!read_file(p, &bytes)) return fail(ER_ERR_IO, "cannot read texture " + mp);
+      int w = 0, h = 0;
+      std::vector<uint8_t> rgb;
+      er_status st = decode_bmp(bytes, p, &w, &h, &rgb);
+      if (st != ER_OK) return st;
+      std::vector<float> f(rgb.size());
+      for (size_t i = 0; i < rgb.size(); i++) f[i] = ldr_to_float(rgb[i], gamma);
+      tex_paths.push_back(mp);
+      F->tex_data.push_back(std::move(f));
+      er_texture t{};
+      t.width = w;
+      t.height = h;
+      t.x_tile = t.y_tile = 1.0f;
+      F->texs.push_back(t);
+    }
+  }
+  for (size_t i = 0; i < F->texs.size(); i++) F->texs[i].data = F->tex_data[i].data();
+  for (const Mtl& mt : mtls) F->mats.push_back(mt.m);
+  if (F->mats.empty()) {  // no .mtl: one default material
+    er_material m;
+    default_material(&m);
+    F->mats.push_back(m);
+  }
+
+  // geometry (SceneLoader.hpp:109-123)
+  if (!read_file(join(dir, "scene.obj"), &text)) return fail(ER_ERR_IO, "cannot read " + join(dir, "scene.obj"));
+  std::vector<Obj> objs;
+  er_status st = parse_obj(text, &objs);
+  if (st != ER_OK) return st;
+  for (size_t o = 0; o < objs.size(); o++) {
+    int mid = 0;
+    for (size_t j = 0; j < mtls.size(); j++)
+      if (mtls[j].name == objs[o].mat) mid = (int)j;
+    F->obj_mat.push_back(mid);
+    size_t nt = objs[o].pos.size() / 9;
+    F->pos.insert(F->pos.end(), objs[o].pos.begin(), objs[o].pos.end());
+    F->nrm.insert(F->nrm.end(), objs[o].nrm.begin(), objs[o].nrm.end());
+    F->uv.insert(F->uv.end(), objs[o].uv.begin(), objs[o].uv.end());
+    F->tri_obj.insert(F->tri_obj.end(), nt, (int32_t)o);
+  }
+  d.tri_count = (int64_t)(F->pos.size() / 9);
+  // tangents per object, as the reference's loader does (ObjLoader.hpp:167-168)
+  F->tan.resize(F->pos.size());
+  F->tsign.resize((size_t)d.tri_count);
+  for (int64_t b = 0, o = 0; b < d.tri_count; o++) {
+    int64_t e = b;
+    while (e < d.tri_count && F->tri_obj[(size_t)e] == o) e++;
+    compute_tangents(e - b, F->pos.data() + 9 * b, F->nrm.data() + 9 * b, F->uv.data() + 6 * b,
+                     F->tan.data() + 9 * b, F->tsign.data() + b);
+    b = e;
+  }
+
+  // point lights (SceneLoader.hpp:125-141)
+  if (const JVal* pl = root.get("pointLights")) {
+    for (const JVal& l : pl->arr) {
+      er_point_light p{};
+      if (!jvec3(l.get("position"), p.position) || !jvec3(l.get("radiance"), p.radiance))
+        return fail(ER_ERR_PARSE, "scene.json: point light needs position and radiance");
+      F->lights.push_back(p);
+    }
+  }
+  d.positions = F->pos.data();
+  d.normals = F->nrm.data();
+  d.uvs = F->uv.data();
+  d.tangents = F->tan.data();
+  d.tangent_sign = F->tsign.data();
+  d.tri_object = F->tri_obj.data();
+  d.object_count = (int32_t)F->obj_mat.size();
+  d.object_material = F->obj_mat.data();
+  d.material_count = (int32_t)F->mats.size();
+  d.materials = F->mats.data();
+  d.texture_count = (int32_t)F->texs.size();
+  d.textures = F->texs.data();
+  d.light_count = (int32_t)F->lights.size();
+  d.lights = F->lights.data();
+  return ER_OK;
+}
+
+}  // namespace
+}  // namespace er
+
 using namespace er;
+
+extern "C" er_status er_scene_folder_read(const char* dir, er_folder** out) {
+  return guarded("er_scene_folder_read", [&]() -> er_status {
+    if (out) *out = nullptr;
+    if (!dir || !out) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+    std::unique_ptr<er_folder> F(new er_folder());
+    er_status st = read_folder(dir, F.get());
+    if (st != ER_OK) return st;
+    *out = F.release();
+    return ER_OK;
+  });
+}
+
+extern "C" er_status er_folder_desc(const er_folder* f, er_scene_desc* out) {
+  if (!f || !out) return fail(ER_ERR_INVALID_ARG, "NULL argument");
+  *out = f->d;
+  return ER_OK;
+}
+
+extern "C" er_status er_folder_free(er_folder* f) {
+  delete f;
+  return ER_OK;
+}
 
 extern "C" er_status er_scene_load(const char* dir_c, const er_scene_opts* opts, er_scene** out) {
   return guarded("er_scene_load", [&]() -> er_status {
     if (out) *out = nullptr;
     if (!dir_c || !out) return fail(ER_ERR_INVALID_ARG, "NULL argument");
-    std::string dir(dir_c);
-    std::string text;
-    if (!read_file(join(dir, "scene.json"), &text)) return fail(ER_ERR_IO, "cannot read " + join(dir, "scene.json"));
-    JVal root;
-    JParser jp(text);
-    if (!jp.val(&root) || root.kind != JVal::OBJ) return fail(ER_ERR_PARSE, "scene.json: malformed JSON");
-
-    er_scene_desc d{};
-    // camera (SceneLoader.hpp:25-46; Camera(xRes, yRes), Camera.hpp:29-37)
-    const JVal* cam = root.get("camera");
-    if (!cam) return fail(ER_ERR_PARSE, "scene.json: no camera");
-    double xr = 0, yr = 0, fl = 0, fd = 0, ap = 0;
-    if (!jnum(cam->get("xRes"), &xr) || !jnum(cam->get("yRes"), &yr))
-      return fail(ER_ERR_PARSE, "scene.json: camera needs xRes and yRes");
-    d.camera.x_res = (int32_t)xr;
-    d.camera.y_res = (int32_t)yr;
-    d.camera.sensor_width = (float)(35 * 0.001);
-    d.camera.sensor_height = d.camera.sensor_width * ((float)d.camera.y_res / (float)d.camera.x_res);
-    d.camera.focal_length = jnum(cam->get("focalLength"), &fl) ? (float)fl : (float)(35 * 0.001);
-    d.camera.focus_distance = jnum(cam->get("focusDistance"), &fd) ? (float)fd : 1000000.0f;
-    d.camera.aperture = jnum(cam->get("aperture"), &ap) ? (float)ap : 2.8f;
-    d.camera.bokeh = jbool(cam->get("bokeh")) ? 1 : 0;
-    if (!jvec3(cam->get("position"), d.camera.position)) std::memset(d.camera.position, 0, sizeof d.camera.position);
-    if (!jvec3(cam->get("rotation"), d.camera.rotation)) std::memset(d.camera.rotation, 0, sizeof d.camera.rotation);
-
-    // environment (SceneLoader.hpp:51-65, HDRI.hpp:22-60)
-    std::vector<float> env_data;
-    const JVal* hd = root.get("hdri");
-    if (!hd) return fail(ER_ERR_PARSE, "scene.json: no hdri");
-    int ew = 0, eh = 0;
-    if (const JVal* nm = hd->get("name")) {
-      std::string hp = join(join(dir, "HDRI"), nm->text + ".hdr");
-      std::string bytes;
-      if (!read_file(hp, &bytes)) return fail(ER_ERR_IO, "cannot read " + hp);
-      er_status st = decode_hdr(bytes, hp, &ew, &eh, &env_data);
-      if (st != ER_OK) return st;
-    } else if (const JVal* col = hd->get("color")) {
-      float c[3];
-      if (!jvec3(col, c)) return fail(ER_ERR_PARSE, "scene.json: hdri.color needs r, g, b");
-      ew = eh = 1024;
-      env_data.resize((size_t)ew * eh * 3);
-      for (size_t i = 0; i < (size_t)ew * eh; i++) { env_data[3 * i] = c[0]; env_data[3 * i + 1] = c[1]; env_data[3 * i + 2] = c[2]; }
-    } else {
-      return fail(ER_ERR_PARSE, "scene.json: hdri needs name or color");
-    }
-    d.env.width = ew;
-    d.env.height = eh;
-    d.env.data = env_data.data();
-    d.env.x_tile = d.env.y_tile = 1.0f;
-    double off = 0;
-    if (jnum(hd->get("xOffset"), &off)) d.env.x_offset = (float)off;
-    if (jnum(hd->get("yOffset"), &off)) d.env.x_offset = (float)off;  // SceneLoader.hpp:64-65
-
-    // materials and textures (SceneLoader.hpp:67-107)
-    std::vector<Mtl> mtls;
-    if (read_file(join(dir, "scene.mtl"), &text)) {
-      er_status st = parse_mtl(text, &mtls);
-      if (st != ER_OK) return st;
-    }
-    std::vector<std::string> tex_paths;
-    std::vector<std::vector<float>> tex_data;
-    std::vector<er_texture> texs;
-    for (Mtl& mt : mtls) {
-      for (auto& kv : mt.maps) {
-        const std::string& key = kv.first;
-        const std::string& mp = kv.second;
-        int id = (int)tex_paths.size();
-        bool dup = false;
-        for (size_t j = 0; j < tex_paths.size(); j++)
-          if (tex_paths[j] == mp) { id = (int)j; dup = true; }
-        float gamma = 1.0f;
-        if (key == "map_Kd") { mt.m.albedo_tex = id; gamma = 2.2f; }
-        if (key == "map_Ns") mt.m.roughness_tex = id;
-        if (key == "refl") mt.m.metallic_tex = id;
-        if (key == "map_Bump") mt.m.normal_tex = id;
-        if (dup) continue;
-        std::string p = file_exists(mp) ? mp : join(dir, mp);
-        std::string bytes;
-        if (!read_file(p, &bytes)) return fail(ER_ERR_IO, "cannot read texture " + mp);
-        int w = 0, h = 0;
-        std::vector<uint8_t> rgb;
-        er_status st = decode_bmp(bytes, p, &w, &h, &rgb);
-        if (st != ER_OK) return st;
-        std::vector<float> f(rgb.size());
-        for (size_t i = 0; i < rgb.size(); i++) f[i] = ldr_to_float(rgb[i], gamma);
-        tex_paths.push_back(mp);
-        tex_data.push_back(std::move(f));
-        er_texture t{};
-        t.width = w;
-        t.height = h;
-        t.x_tile = t.y_tile = 1.0f;
-        texs.push_back(t);
-      }
-    }
-    for (size_t i = 0; i < texs.size(); i++) texs[i].data = tex_data[i].data();
-    std::vector<er_material> mats;
-    for (const Mtl& mt : mtls) mats.push_back(mt.m);
-    if (mats.empty()) {  // no .mtl: one default material
-      er_material m;
-      default_material(&m);
-      mats.push_back(m);
-    }
-
-    // geometry (SceneLoader.hpp:109-123)
-    if (!read_file(join(dir, "scene.obj"), &text)) return fail(ER_ERR_IO, "cannot read " + join(dir, "scene.obj"));
-    std::vector<Obj> objs;
-    er_status st = parse_obj(text, &objs);
+    er_folder F;
+    er_status st = read_folder(dir_c, &F);
     if (st != ER_OK) return st;
-    std::vector<float> pos, nrm, uv;
-    std::vector<int32_t> tri_obj, obj_mat;
-    for (size_t o = 0; o < objs.size(); o++) {
-      int mid = 0;
-      for (size_t j = 0; j < mtls.size(); j++)
-        if (mtls[j].name == objs[o].mat) mid = (int)j;
-      obj_mat.push_back(mid);
-      size_t nt = objs[o].pos.size() / 9;
-      pos.insert(pos.end(), objs[o].pos.begin(), objs[o].pos.end());
-      nrm.insert(nrm.end(), objs[o].nrm.begin(), objs[o].nrm.end());
-      uv.insert(uv.end(), objs[o].uv.begin(), objs[o].uv.end());
-      tri_obj.insert(tri_obj.end(), nt, (int32_t)o);
-    }
-    d.tri_count = (int64_t)(pos.size() / 9);
-    d.positions = pos.data();
-    d.normals = nrm.data();
-    d.uvs = uv.data();
-    // tangents per object, as the reference's loader does (ObjLoader.hpp:167-168)
-    std::vector<float> tan(pos.size()), tsign((size_t)d.tri_count);
-    for (int64_t b = 0, o = 0; b < d.tri_count; o++) {
-      int64_t e = b;
-      while (e < d.tri_count && tri_obj[(size_t)e] == o) e++;
-      compute_tangents(e - b, pos.data() + 9 * b, nrm.data() + 9 * b, uv.data() + 6 * b, tan.data() + 9 * b,
-                       tsign.data() + b);
-      b = e;
-    }
-    d.tangents = tan.data();
-    d.tangent_sign = tsign.data();
-    d.tri_object = tri_obj.data();
-    d.object_count = (int32_t)obj_mat.size();
-    d.object_material = obj_mat.data();
-    d.material_count = (int32_t)mats.size();
-    d.materials = mats.data();
-    d.texture_count = (int32_t)texs.size();
-    d.textures = texs.data();
-
-    // point lights (SceneLoader.hpp:125-141)
-    std::vector<er_point_light> lights;
-    if (const JVal* pl = root.get("pointLights")) {
-      for (const JVal& l : pl->arr) {
-        er_point_light p{};
-        if (!jvec3(l.get("position"), p.position) || !jvec3(l.get("radiance"), p.radiance))
-          return fail(ER_ERR_PARSE, "scene.json: point light needs position and radiance");
-        lights.push_back(p);
-      }
-    }
-    d.light_count = (int32_t)lights.size();
-    d.lights = lights.data();
-    return er_scene_create(&d, opts, out);
+    return er_scene_create(&F.d, opts, out);
   });
 }

@@ -47,6 +47,12 @@ def load(build_if_missing=True):
     L.er_scene_create.argtypes = [C.POINTER(A.er_scene_desc), C.POINTER(A.er_scene_opts), C.POINTER(C.c_void_p)]
     L.er_scene_load.restype = A.er_status
     L.er_scene_load.argtypes = [C.c_char_p, C.POINTER(A.er_scene_opts), C.POINTER(C.c_void_p)]
+    L.er_scene_folder_read.restype = A.er_status
+    L.er_scene_folder_read.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    L.er_folder_desc.restype = A.er_status
+    L.er_folder_desc.argtypes = [C.c_void_p, C.POINTER(A.er_scene_desc)]
+    L.er_folder_free.restype = A.er_status
+    L.er_folder_free.argtypes = [C.c_void_p]
     L.er_scene_info_get.restype = A.er_status
     L.er_scene_info_get.argtypes = [C.c_void_p, C.POINTER(A.er_scene_info)]
     L.er_scene_set_camera.restype = A.er_status
@@ -106,6 +112,8 @@ def load(build_if_missing=True):
     L.er_postprocess.restype = A.er_status
     L.er_postprocess.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(A.er_post_opts), C.c_void_p,
                                  C.c_void_p, C.c_uint32]
+    L.er_device_bandwidth.restype = A.er_status
+    L.er_device_bandwidth.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_double)]
     L.er_write_image.restype = A.er_status
     L.er_write_image.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     _lib = L
@@ -119,6 +127,48 @@ def check(status, where):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def read_folder(path):
+    """Parse a scene folder on the host (er_scene_folder_read): a dict of
+    numpy copies of the description's arrays (no device needed)."""
+    L = load()
+    h = C.c_void_p()
+    check(L.er_scene_folder_read(os.fsencode(str(path)), C.byref(h)), "er_scene_folder_read")
+    try:
+        d = A.er_scene_desc()
+        check(L.er_folder_desc(h, C.byref(d)), "er_folder_desc")
+        T = int(d.tri_count)
+
+        def arr(ptr, n, dt):
+            if not ptr or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), (n,)).copy()
+
+        out = dict(
+            camera=d.camera,
+            positions=arr(d.positions, 9 * T, np.float32).reshape(T, 3, 3),
+            normals=arr(d.normals, 9 * T, np.float32).reshape(T, 3, 3),
+            uvs=arr(d.uvs, 6 * T, np.float32).reshape(T, 3, 2),
+            tangents=arr(d.tangents, 9 * T, np.float32).reshape(T, 3, 3),
+            tangent_sign=arr(d.tangent_sign, T, np.float32),
+            tri_object=arr(d.tri_object, T, np.int32),
+            object_material=arr(d.object_material, d.object_count, np.int32),
+            materials=[A.er_material.from_buffer_copy(d.materials[i]) for i in range(d.material_count)],
+            lights=[A.er_point_light.from_buffer_copy(d.lights[i]) for i in range(d.light_count)],
+        )
+        texs = []
+        for i in range(d.texture_count):
+            t = d.textures[i]
+            texs.append(arr(t.data, 3 * t.width * t.height, np.float32).reshape(t.height, t.width, 3))
+        out["textures"] = texs
+        e = d.env
+        out["env"] = arr(e.data, 3 * e.width * e.height, np.float32).reshape(e.height, e.width, 3)
+        out["env_offset"] = (float(e.x_offset), float(e.y_offset))
+        out["env_tile"] = (float(e.x_tile), float(e.y_tile))
+        return out
+    finally:
+        L.er_folder_free(h)
 
 
 class Scene:
@@ -377,3 +427,11 @@ def postprocess(rgba, width, height, exposure=1.0, tonemap=0, clamp=False, srgb=
 def write_image(path, rgba_u8, width, height, as_bmp=False):
     rgba_u8 = np.ascontiguousarray(rgba_u8, np.uint8)
     check(load().er_write_image(os.fsencode(path), _p(rgba_u8), width, height, int(as_bmp)), "er_write_image")
+
+
+def device_bandwidth(kind, nbytes, reps, device=0):
+    """GB/s measured by er_device_bandwidth (kind: A.ER_BW_L2_READ or
+    A.ER_BW_HBM_COPY)."""
+    g = C.c_double()
+    check(load().er_device_bandwidth(device, kind, nbytes, reps, C.byref(g)), "er_device_bandwidth")
+    return g.value

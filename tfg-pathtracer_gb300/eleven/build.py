@@ -23,7 +23,10 @@ LIB = os.path.join(PKG_ROOT, "libeleven.so")
 CLI = os.path.join(PKG_ROOT, "bin", "eleven")  # the command-line renderer
 INCLUDE = os.path.join(ROOT, "include")
 ORACLE = os.path.join(ROOT, "oracle")
-REF_SRC = os.environ.get("ELEVEN_REF_DIR", "/root/reference/src/tfg-pathtracer")
+# the reference tree: an unmodified copy in baseline/_ref/ (git-ignored; made
+# by `make -C oracle ref-copy` where the original exists, and carried with the
+# working tree to the GPU machine)
+REF_SRC = os.environ.get("ELEVEN_REF_DIR", os.path.join(ROOT, "baseline", "_ref", "src", "tfg-pathtracer"))
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -38,7 +41,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "--fma
 CU_FLAGS += os.environ.get("ELEVEN_NVCC_FLAGS", "").split()
 
 SOURCES = ["capi.cpp", "scene.cpp", "bvh_build.cpp", "loader.cpp", "tangents.cpp",
-           "trace.cu", "render.cu", "env.cu", "batch.cu", "adjoint.cu", "post.cu", "bvh_gpu.cu"]
+           "trace.cu", "render.cu", "env.cu", "batch.cu", "adjoint.cu", "post.cu", "bvh_gpu.cu", "probe.cu"]
 
 
 def _run(cmd, cwd=None):
@@ -101,8 +104,20 @@ def build_oracle(force=False):
     return target
 
 
+def copy_ref():
+    """Makes the baseline/_ref/ copy of the reference tree where the original
+    is present (the Makefile names its location); no-op otherwise."""
+    if os.path.isdir(REF_SRC) or "ELEVEN_REF_DIR" in os.environ:
+        return
+    r = subprocess.run(["make", "-s", "-C", ORACLE, "ref-copy"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       text=True)
+    if r.returncode != 0 and os.path.isdir(REF_SRC):
+        raise RuntimeError("reference copy failed:\n" + r.stdout)
+
+
 def build_ref(force=False):
     """Reference headers through oracle/ref_shim.cpp; only where they exist."""
+    copy_ref()
     if not os.path.isdir(REF_SRC):
         return None
     args = ["make", "-s", "-C", ORACLE, "ref", "REF_DIR=" + REF_SRC]
