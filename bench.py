@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="c1: skip the batched (64-job) and adjoint sub-records of the default line")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="--impl reference: skip timing the reference's CUDA renderer on the GPU")
     ap.add_argument("--launch-rays", type=int, default=-1,
@@ -188,6 +190,46 @@ def traffic_per_ray():
         return json.load(f)
 
 
+def l2_roofline(config, rays, trace_launches, trace_ms, hits, shade_ms, shade_launches, device):
+    """L2 and DRAM bytes of k_trace / k_shade per ray / per hit from the
+    committed ncu capture (profiles/l2_dram_c1.json), scaled to the live
+    launches, against this GPU's L2 read ceiling measured by the library."""
+    from eleven import _abi as A
+    from eleven import _lib
+    try:
+        l2_peak = _lib.device_bandwidth(A.ER_BW_L2_READ, 64 << 20, 40, device)
+        hbm_own = _lib.device_bandwidth(A.ER_BW_HBM_COPY, 1 << 30, 4, device)
+    except Exception as e:  # noqa: BLE001
+        return {"l2": {"unavailable": str(e)}}
+    p = os.path.join(ROOT, "profiles", "l2_dram_c1.json")
+    prof = json.load(open(p)) if os.path.exists(p) else None
+    res = {"peak_l2_read": round(l2_peak, 1), "peak_hbm_copy_own_kernel": round(hbm_own, 1), "unit": "GB/s",
+           "peak_source": "er_device_bandwidth on this GPU (64 MiB L2-resident read x40; 1 GiB copy x4)"}
+    if prof and prof.get("config") == config:
+        t, sh = prof["k_trace"], prof["k_shade"]
+        tl = trace_ms * 1e-3 / max(trace_launches, 1)
+        per_launch = rays / max(trace_launches, 1)
+        res["k_trace"] = {"l2_bytes_per_ray": round(t["lts_bytes"] / t["rays"], 1),
+                          "achieved_l2": round(t["lts_bytes"] / t["rays"] * per_launch / tl / 1e9, 1),
+                          "dram_bytes_per_ray": round(t["dram_bytes"] / t["rays"], 1),
+                          "achieved_dram": round(t["dram_bytes"] / t["rays"] * per_launch / tl / 1e9, 1)}
+        res["k_trace"]["frac_l2"] = round(res["k_trace"]["achieved_l2"] / l2_peak, 4)
+        sl = shade_ms * 1e-3 / max(shade_launches, 1)
+        hp = hits / max(shade_launches, 1)
+        res["k_shade"] = {"l2_bytes_per_hit": round(sh["lts_bytes"] / sh["hits"], 1),
+                          "achieved_l2": round(sh["lts_bytes"] / sh["hits"] * hp / sl / 1e9, 1),
+                          "dram_bytes_per_hit": round(sh["dram_bytes"] / sh["hits"], 1),
+                          "achieved_dram": round(sh["dram_bytes"] / sh["hits"] * hp / sl / 1e9, 1)}
+        res["k_shade"]["frac_l2"] = round(res["k_shade"]["achieved_l2"] / l2_peak, 4)
+        for k in ("issue_active", "simt_efficiency"):
+            if k in t:
+                res["k_trace"][k] = t[k]
+            if k in sh:
+                res["k_shade"][k] = sh[k]
+        res["source"] = "profiles/l2_dram_c1.json (" + prof.get("command", "") + ")"
+    return {"l2": res}
+
+
 def cpu_baseline(arrays, max_depth, seconds, seed=0):
     """Oracle port of the reference on all host threads, bounded pixel subset."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -239,6 +281,12 @@ def reference_cuda(arrays, max_depth, warm, spp):
     from eleven.build import ORACLE, REF_SRC
     if not os.path.isdir(REF_SRC):
         return {"unavailable": "reference sources not present"}
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device visible"}
+    except ImportError:
+        pass
     t = time.perf_counter()
     r = subprocess.run(["make", "-s", "-C", ORACLE, "-j4", "refcuda", "REF_DIR=" + REF_SRC], capture_output=True,
                        text=True)
@@ -389,6 +437,10 @@ def run_gpu(args):
     if tr and tr.get("kernel") == kname and args.config == tr.get("config"):
         traffic = tr["dram_bytes_per_ray"] * rays / max(nl, 1)
     stage = {n: round(pst.stage_ms[k] / prof_steps, 3) for k, n in enumerate(A.STAGES)}
+    # L2 side of the same kernels: L2 bytes (lts__t_bytes) per ray / per hit
+    # from one ncu capture each, over the live launch times, against the L2
+    # read ceiling the library measures on this GPU (er_device_bandwidth)
+    l2 = l2_roofline(args.config, rays, nl, kms, pst.path_vertices, pst.stage_ms[2], pst.stage_launches[2], local)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -406,7 +458,8 @@ def run_gpu(args):
                      "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "algorithmic_bytes_per_ray": round(b_ray, 1),
                      "launches": int(nl), "avg_launch_ms": round(kms / max(nl, 1), 4),
-                     "timing": f"CUDA events after every launch, profiled pass of {prof_steps} steps on one stream"},
+                     "timing": f"CUDA events after every launch, profiled pass of {prof_steps} steps on one stream",
+                     **l2},
         "rays_per_s": {"closest": round(st.rays_closest / ms / 1e3, 1), "shadow": round(st.rays_shadow / ms / 1e3, 1),
                        "unit": "Mrays/s"},
         "path_vertices_per_s": round(st.path_vertices / ms / 1e3, 1),
@@ -424,6 +477,18 @@ def run_gpu(args):
         cb, _ = cpu_baseline(arrays, max_depth, args.cpu_seconds)
         line["cpu_baseline"] = cb
     scene.close()
+    if rank == 0 and world == 1 and args.config == "c1" and not args.no_sub:
+        # the other two parts of the headline metric, measured in the same
+        # run: the batched 8-bit-BVH form against the plain tracer on the
+        # 64-job workload, and adjoint full-gradient evaluations per second
+        b = measure_batch(args.jobs, 2, 1)
+        line["batched"] = {k: b[k] for k in ("metric", "value", "unit", "steps", "ms_per_step", "config", "plain",
+                                              "batched", "speedup_batched_vs_plain", "films_bit_identical", "clocks")
+                           if k in b}
+        a = measure_adjoint(3, 1, args.fd_params)
+        line["adjoint"] = {k: a[k] for k in ("metric", "value", "unit", "ms_per_step", "config", "forward_ms",
+                                             "backward_ms", "backward_msamples_per_s", "fd_check", "clocks")
+                           if k in a}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:
@@ -432,6 +497,12 @@ def run_gpu(args):
 
 
 def run_batch(args):
+    line = measure_batch(args.jobs, args.steps, args.warmup)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_batch(n_jobs, steps, warmup):
     """c2: 64 heterogeneous scenes/views.  Plain = each job through er_render
     on its own scene, one after another (FP32 BVH); batched = all jobs in one
     er_batch (8-bit BVH, autotuned schedule, one CUDA graph per render).  A
@@ -440,7 +511,7 @@ def run_batch(args):
     from eleven import _abi as A
     from eleven import _lib, scenes
     t_gen = time.perf_counter()
-    arrays, jobs = scenes.config2(n_jobs=args.jobs)
+    arrays, jobs = scenes.config2(n_jobs=n_jobs)
     t_gen = time.perf_counter() - t_gen
     t_build = time.perf_counter()
     plain = [_lib.Scene(a) for a in arrays]
@@ -454,25 +525,25 @@ def run_batch(args):
             ms += s.render(j["spp"], max_depth=j["max_depth"], seed=j["seed"], flags=flags)["stats"].ms
         return ms
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         plain_pass()
     clocks = Clocks(0)
     clocks.start()
     time.sleep(0.3)
     t0 = time.perf_counter()
-    plain_ms = [plain_pass() for _ in range(args.steps)]
-    plain_wall = (time.perf_counter() - t0) / args.steps
+    plain_ms = [plain_pass() for _ in range(steps)]
+    plain_wall = (time.perf_counter() - t0) / steps
 
     b = _lib.Batch(q8, bvh_format=A.ER_BVH_Q8)
     b.set_jobs(jobs)
     t_tune = time.perf_counter()
     tuning = b.autotune(reps=1)
     t_tune = time.perf_counter() - t_tune
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         b.render()
     t0 = time.perf_counter()
-    stats = [b.render() for _ in range(args.steps)]
-    batch_wall = (time.perf_counter() - t0) / args.steps
+    stats = [b.render() for _ in range(steps)]
+    batch_wall = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
     batch_ms = [s.ms for s in stats]
     # same films: compare a few jobs with the plain renders (host output)
@@ -485,7 +556,7 @@ def run_batch(args):
     pm, bm = float(np.median(plain_ms)), float(np.median(batch_ms))
     line = {
         "metric": "Msamples/s, 64-job batch (batched 8-bit BVH vs plain sequential)", "value": round(samples / bm / 1e3, 3),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(bm, 3),
+        "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": round(bm, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, reference scene shapes)",
         "config": {"workload": f"c2: {len(jobs)} jobs, resolutions 128^2..1024x768, spp 4/16/64, depth 4-8, "
@@ -511,11 +582,16 @@ def run_batch(args):
     b.close()
     for s in plain + q8:
         s.close()
+    return line
+
+
+def run_adjoint(args):
+    line = measure_adjoint(args.steps, args.warmup, args.fd_params)
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_adjoint(args):
+def measure_adjoint(steps, warmup, fd_params):
     """c4: gradients of an L2 image loss with respect to 98,624 parameters
     (64 objects x 5 Disney parameters + a 256x128 RGB environment), 512x512,
     64 spp forward + 64 spp path-replay adjoint, max depth 6.  A step is one
@@ -543,14 +619,14 @@ def run_adjoint(args):
         gm, ge, st = s.backward(spp, d, out["samples"], max_depth=depth, seed=seed)
         return out["stats"].ms, st.ms, gm, ge
 
-    for w in range(max(1, args.warmup)):
+    for w in range(max(1, warmup)):
         step(1000 + w)
     clocks = Clocks(0)
     clocks.start()
     time.sleep(0.3)
     t0 = time.perf_counter()
-    res = [step(k) for k in range(args.steps)]
-    wall = (time.perf_counter() - t0) / args.steps
+    res = [step(k) for k in range(steps)]
+    wall = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
     fwd = float(np.median([r[0] for r in res]))
     bwd = float(np.median([r[1] for r in res]))
@@ -567,7 +643,7 @@ def run_adjoint(args):
     gm, ge, _ = s.backward(fspp, d, out["samples"], max_depth=depth, seed=5)
     g = np.concatenate([gm.ravel(), ge.ravel()])
     rng = np.random.default_rng(32)
-    idx = rng.choice(n_params, args.fd_params, replace=False)
+    idx = rng.choice(n_params, fd_params, replace=False)
 
     def loss(img):
         dd = img[:, :3].astype(np.float64) - T[:, :3].astype(np.float64)
@@ -592,15 +668,15 @@ def run_adjoint(args):
     s.close()
     line = {
         "metric": "adjoint full-gradient evaluations/s (512x512, 64 spp forward + 64 spp replay, depth 6)",
-        "value": round(1e3 / (fwd + bwd), 4), "unit": "grads/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(fwd + bwd, 2), "higher_is_better": True, "scaling": "weak",
+        "value": round(1e3 / (fwd + bwd), 4), "unit": "grads/s", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(fwd + bwd, 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, reference scene shapes)",
         "config": {"workload": "c4: 64 icospheres (1280 tris each), 1 point light, 256x128 log-normal env; "
                                "L2 loss to a render with other seeded parameters",
                    "parameters": int(n_params), "spp": spp, "max_depth": depth},
         "forward_ms": round(fwd, 2), "backward_ms": round(bwd, 2), "replay_forward_wall_ms": round(replay_ms, 1), "wall_ms_per_step": round(wall * 1e3, 2),
         "backward_msamples_per_s": round(512 * 512 * spp / bwd / 1e3, 2),
-        "fd_check": {"params": int(args.fd_params), "checked": len(errs), "negligible": skipped,
+        "fd_check": {"params": int(fd_params), "checked": len(errs), "negligible": skipped,
                      "max_rel_err": round(float(max(errs)) if errs else 0.0, 6),
                      "median_rel_err": round(float(np.median(errs)) if errs else 0.0, 6),
                      "h": h, "spp": fspp, "estimator": "detached sampling (er_render_replay)"},
@@ -608,8 +684,7 @@ def run_adjoint(args):
     }
     if clk:
         line["clocks"] = clk
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def launch_rays(args):
