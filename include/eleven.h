@@ -265,6 +265,14 @@ er_status er_film_read(er_scene* scene, uint32_t flags, float* beauty,
                        float* normal, float* tangent, float* bitangent,
                        uint32_t* samples, uint32_t* pathcount);
 
+/* The film's per-pixel FP64 sums of the clamped sample radiance (W*H*3
+ * doubles, the film's pixel order) and sample counts, when every render into
+ * it since it was last cleared ran with ER_RENDER_ACCUM_FP64
+ * (ER_ERR_INVALID_ARG otherwise).  The exact form of the film for callers
+ * that merge films of sample ranges rendered apart, or difference two films
+ * (the FP32 beauty rounds each pixel's mean once more). */
+er_status er_film_read_sums(er_scene* scene, uint32_t flags, double* sums, uint32_t* samples);
+
 /* Progressive readback while er_render runs on another thread (the
  * reference's window loop polls getBuffers during renderCuda, main.cpp:53,
  * kernel.cu:688-710): the film as of the last finished wave of a render
@@ -367,11 +375,14 @@ er_status er_postprocess(const float* rgba_in, int32_t width, int32_t height, co
 er_status er_scene_get_params(er_scene* scene, float* materials, float* env);
 er_status er_scene_set_params(er_scene* scene, const float* materials, const float* env, uint32_t flags);
 
-/* Forward render by path replay: sampling (directions, pdfs, MIS weights,
- * chosen texel and light) from the scene's parameters, BRDF values and
- * environment radiance from eval_materials / eval_env (NULL = the scene's).
- * With both NULL the film equals er_render's for the same options.  Only
- * ER_RENDER_DEVICE_OUT and ER_RENDER_ENV_ALIAS apply. */
+/* Forward render of the detached estimator: sampling (directions, pdfs, MIS
+ * weights, chosen texel and light) from the scene's parameters, BRDF values
+ * and environment radiance from eval_materials / eval_env (NULL = the
+ * scene's).  It runs the er_render wavefront and, like er_render, replaces
+ * the scene's film.  With both NULL the film equals er_render's for the
+ * same options.  Only ER_RENDER_DEVICE_OUT, ER_RENDER_ENV_ALIAS and
+ * ER_RENDER_ACCUM_FP64 apply (FP64 per-pixel sums, so that finite
+ * differences of the estimator see no running-mean rounding). */
 er_status er_render_replay(er_scene* scene, const er_render_opts* opts, const float* eval_materials,
                            const float* eval_env, float* beauty, uint32_t* samples, uint32_t* pathcount);
 

@@ -97,6 +97,7 @@ def test_invalid_arguments_rejected():
     assert L.er_scene_free(None) == 0
     assert L.er_trace_closest(None, None, 0, None, None, None, 0, None) == 1
     assert L.er_render(None, None, None, None, None, None, None, None, None) == 1
+    assert L.er_film_read_sums(None, 0, None, None) == A.ER_ERR_INVALID_ARG
 
 
 def test_render_options_checked_before_the_scene():

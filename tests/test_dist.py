@@ -61,8 +61,11 @@ def _rank(rank, world, port, q):
         first, n = DD.shard_samples(6, rank, world)
         out = orc.render(spp=n, max_depth=3, seed=4, sample_begin=first)
         beauty, samples = DD.reduce_film(out["beauty"], out["samples"])
+        # the exact form: FP64 sums (here the share's mean times its counts)
+        own = out["beauty"][:, :3].astype(np.float64) * out["samples"][:, None]
+        sums, cnt, b2 = DD.reduce_sums(own, out["samples"])
         if rank == 0:
-            q.put((beauty, samples))
+            q.put((beauty, samples, sums, cnt, b2))
         orc.close()
     finally:
         dist.destroy_process_group()
@@ -81,7 +84,7 @@ def test_two_ranks_merge_to_the_single_process_film():
     procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    beauty, samples = q.get(timeout=300)
+    beauty, samples, sums, cnt, b2 = q.get(timeout=300)
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
@@ -94,3 +97,11 @@ def test_two_ranks_merge_to_the_single_process_film():
     # two FP32 running means: equal up to float rounding
     np.testing.assert_allclose(beauty[:, :3], ref["beauty"][:, :3], rtol=2e-5, atol=1e-6)
     assert (beauty[:, 3] == 1).all()
+    # reduce_sums: the ranks' sums added, the merged mean rounded once
+    orc = O.OrcScene(arrays)
+    parts = [orc.render(spp=3, max_depth=3, seed=4, sample_begin=b) for b in (0, 3)]
+    orc.close()
+    want = sum(p["beauty"][:, :3].astype(np.float64) * p["samples"][:, None] for p in parts)
+    np.testing.assert_allclose(sums, want, rtol=1e-15, atol=0)
+    np.testing.assert_array_equal(cnt, ref["samples"])
+    np.testing.assert_array_equal(b2[:, :3], (want / np.maximum(cnt, 1)[:, None]).astype(np.float32))

@@ -6,9 +6,9 @@
 - Differentiation scene in full: 512x512, 64 icospheres, 256x128 env,
   max depth 6, 98,624 parameters.  The adjoint gradient at 4096 samples per
   pixel against central finite differences (h = 1e-3, the same 4096 samples:
-  common random numbers) of the detached estimator on 32 random parameters,
-  relative error below 1e-2; then 100 Adam steps (lr 1e-2, 64 spp) lower
-  the loss.  The clamp of kernel.cu:447 and the 2.2 power of
+  common random numbers) of the detached estimator on 32 random parameters
+  where it is differentiable, relative error below 1e-2; then 100 Adam
+  steps (lr 1e-2, 64 spp) lower the loss.  The clamp of kernel.cu:447 and the 2.2 power of
   kernel.cu:103-104 are inside the differentiated estimator.
 """
 import numpy as np
@@ -88,7 +88,27 @@ def _loss(beauty, T):
     return float((d * d).sum())
 
 
+def _loss_exact(sums, samples, T):
+    """The loss of the film's exact (FP64) pixel means."""
+    img = sums / np.maximum(samples, 1)[:, None]
+    d = img - T[:, :3].astype(np.float64)
+    return float((d * d).sum())
+
+
 def test_c4_full_gradient_matches_fd_4096spp(c4_full):
+    """32 random parameters: 16 of the 256 albedo and roughness parameters
+    and 16 of the 98,304 environment texel channels.  The metallic
+    parameters are excluded: the configuration draws them from {0, 1}, where
+    the estimator is not differentiable (below 0 the 2.2 power of
+    kernel.cu:104 is undefined; at 1 the diffuse lobe's (1 - metallic)
+    changes sign and the samples it alone lights are clamped at 0 on one
+    side, kernel.cu:447), so a central difference there does not estimate
+    the gradient.  The finite differences are taken of the films' FP64 sums
+    (ER_RENDER_ACCUM_FP64, er_film_read_sums): neither the FP32 running mean
+    nor the final rounding of each pixel to float enters the differences,
+    whose step of 1e-3 would otherwise move the loss by less than that
+    rounding for the smaller gradients."""
+    from eleven import _abi as A
     arrays, s, T = c4_full
     spp, h, seed = 4096, 1e-3, 5
     m0, e0 = s.get_params()
@@ -99,11 +119,10 @@ def test_c4_full_gradient_matches_fd_4096spp(c4_full):
     g = np.concatenate([gm.ravel(), ge.ravel()]).astype(np.float64)
     assert np.isfinite(g).all()
     gmax = np.abs(g).max()
-    # 32 random parameters: 16 of the 320 material parameters and 16 of the
-    # 98,304 environment texel channels
     rng = np.random.default_rng(32)
-    idx = list(rng.choice(m0.size, 16, replace=False)) + list(m0.size + rng.choice(e0.size, 16, replace=False))
-    rows, checked = [], 0
+    smooth = np.nonzero(np.arange(m0.size) % 5 != 4)[0]  # albedo r, g, b and roughness
+    idx = list(rng.choice(smooth, 16, replace=False)) + list(m0.size + rng.choice(e0.size, 16, replace=False))
+    rows = []
     for k in idx:
         vals = []
         for sign in (1, -1):
@@ -112,19 +131,19 @@ def test_c4_full_gradient_matches_fd_4096spp(c4_full):
                 m.ravel()[k] += sign * h
             else:
                 e.ravel()[k - m0.size] += sign * h
-            vals.append(_loss(s.render_replay(spp, max_depth=C4_DEPTH, seed=seed, materials=m, env=e)["beauty"], T))
+            s.render_replay(spp, max_depth=C4_DEPTH, seed=seed, materials=m, env=e, flags=A.ER_RENDER_ACCUM_FP64)
+            vals.append(_loss_exact(*s.read_sums(), T))
         fd = (vals[0] - vals[1]) / (2 * h)
         big = max(abs(fd), abs(g[k]))
-        rel = abs(fd - g[k]) / big if big > 0 else 0.0
-        rows.append((int(k), float(g[k]), fd, rel))
-        # parameters whose gradient is below 1e-5 of the largest one move the
-        # loss by less than its FP32 rounding: reported, not checked
-        if big >= 1e-5 * gmax:
-            checked += 1
-            assert rel < 1e-2, f"param {k}: adjoint {g[k]:.6g} vs finite difference {fd:.6g} (rel {rel:.3g})"
+        rows.append((int(k), float(g[k]), fd, abs(fd - g[k]) / big if big > 0 else 0.0, big))
     print("\nc4 full, 4096 spp: (param, adjoint, finite difference, rel) " +
-          "; ".join(f"{k} {a:.4g} {b:.4g} {r:.2e}" for k, a, b, r in rows))
-    assert checked >= 20, f"only {checked} of 32 parameters above the noise floor"
+          "; ".join(f"{k} {a:.5g} {b:.5g} {r:.2e}" for k, a, b, r, _ in rows))
+    # parameters whose gradient is below 1e-7 of the largest one: reported,
+    # not checked
+    checked = [r for r in rows if r[4] >= 1e-7 * gmax]
+    bad = [r for r in checked if r[3] >= 1e-2]
+    assert not bad, f"relative error >= 1e-2: {bad}"
+    assert len(checked) >= 28, f"only {len(checked)} of 32 parameters above the noise floor"
 
 
 def test_c4_full_adam_100_steps(c4_full):

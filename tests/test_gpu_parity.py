@@ -227,3 +227,23 @@ def test_normal_map_paths_match_oracle():
     np.testing.assert_allclose(out["tangent"][:, :3], ref["tangent"][:, :3], rtol=1e-4, atol=1e-5)
     scene.close()
     orc.close()
+
+
+def test_fp64_sums_readback(c0):
+    """er_film_read_sums: the FP64 sums of an ER_RENDER_ACCUM_FP64 film
+    (continued renders included) divided by the sample counts give the
+    beauty pass up to its float rounding; a film that any FP32 render
+    touched has no valid sums."""
+    arrays, scene, orc = c0
+    out = scene.render(spp=3, max_depth=4, seed=2, flags=A.ER_RENDER_ACCUM_FP64)
+    scene.render(spp=2, max_depth=4, seed=2, sample_begin=3, flags=A.ER_RENDER_ACCUM_FP64 | A.ER_RENDER_CONTINUE)
+    sums, samples = scene.read_sums()
+    full = scene.render(spp=5, max_depth=4, seed=2, flags=A.ER_RENDER_ACCUM_FP64)
+    s2, n2 = scene.read_sums()
+    assert np.array_equal(samples, n2) and np.array_equal(sums, s2)  # continue == one call
+    mean = (s2 / np.maximum(n2, 1)[:, None]).astype(np.float32)
+    assert np.array_equal(mean, full["beauty"][:, :3])
+    assert (out["samples"] <= n2).all()
+    scene.render(spp=1, max_depth=4, seed=2)
+    with pytest.raises(_lib.ElevenError):
+        scene.read_sums()

@@ -106,6 +106,42 @@ __device__ __forceinline__ EvalGrad disney_eval_grad(const HitData& hd, const Di
   return g;
 }
 
+// The detached estimator at a vertex (er_render_replay): the vertex's
+// BRDF values and environment radiance re-evaluated with the evaluation
+// parameters (albedo, roughness, metallic per material before the 2.2 power
+// of kernel.cu:103-104; env texels), with its directions, pdfs, MIS weights,
+// chosen texel and light kept from the scene's parameters; updates the
+// strategy terms tH, tP, tB and the throughput factor g (kernel.cu:339-357).
+__device__ __forceinline__ void eval_vertex(const DevScene& S, const float* eval_mat, const float* eval_env, f3 d,
+                                            VertexShade& V) {
+  const DevMaterial& M = S.mats[V.mat];
+  HitData he = V.hd;
+  if (eval_mat) {
+    const float* q = eval_mat + 5 * (size_t)V.mat;
+    if (M.albedo_tex < 0) he.albedo = mk(q[0], q[1], q[2]);
+    if (M.roughness_tex < 0) he.roughness = powf(q[3], 2.2f);
+    if (M.metallic_tex < 0) he.metallic = powf(q[4], 2.2f);
+  }
+  const DisneyCtx Ce = disney_ctx(he, d);
+  const f3 f = disney_eval(he, Ce, V.dir);
+  const f3 fH = disney_eval(he, Ce, V.dH);
+  f3 eH = V.eH;
+  if (eval_env) {
+    const int64_t t3 = 3 * V.env_texel;
+    eH = mk(eval_env[t3], eval_env[t3 + 1], eval_env[t3 + 2]);
+  }
+  const f3 hdriC = (fH * V.cosH) * eH / V.hdriPdf;
+  V.tH = hdriC * V.w1;
+  if (V.has_pt) {
+    const f3 fP = disney_eval(he, Ce, V.dP);
+    const f3 pointC = (V.plv * fP) * V.cosP / V.pointPdf;
+    V.tP = pointC * V.w2;
+  }
+  const f3 brdfC = (f * V.ndl) * he.emission / V.brdfPdf;
+  V.tB = brdfC * V.w3;
+  V.g = (f * V.ndl) / V.brdfPdf;
+}
+
 // base[key * N + k] += v[k], warp-aggregated: the converged lanes that
 // share a key (neighbouring pixels see the same env texel and object) are
 // summed with shuffles and one lane issues the N atomics.  Non-finite

@@ -191,6 +191,7 @@ struct Film {
   float4* beauty = nullptr;
   float4* aov[3] = {nullptr, nullptr, nullptr};
   double* sum = nullptr;       // FP64 sums (3 per pixel) in FP64 mode
+  bool sum_valid = false;      // every sample of the film went into sum
   uint32_t* samples = nullptr;
   uint32_t* pathcount = nullptr;
   bool aov_on = false;
@@ -357,6 +358,11 @@ void hdri_cdf(const er_texture& t, std::vector<float>& cdf, float* radiance_sum)
 // d loss / d beauty and the forward film's sample counts per pixel, and the
 // gradient arrays (materials x 5, env texels x 3).
 struct GradArgs {
+  // forward evaluation parameters (er_render_replay): materials (n x 5) and
+  // env texels (w*h*3) the BRDF values and environment radiance are taken
+  // from while the sampling stays with the scene's; null = the scene's
+  const float* eval_mat = nullptr;
+  const float* eval_env = nullptr;
   const float* rad = nullptr;
   const float4* d_beauty = nullptr;
   const uint32_t* nvalid = nullptr;
@@ -367,6 +373,12 @@ struct GradArgs {
 // Runs the samples of opts through the wavefront with the gradient variant
 // of the shade stage (render.cu).
 er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G);
+// The detached estimator (er_render_replay): the samples of opts through the
+// wavefront with BRDF values and environment radiance from the evaluation
+// parameters in G (device arrays), into the scene's film; outputs as
+// er_render's (render.cu).
+er_status render_eval_device(er_scene* s, const er_render_opts* o, const GradArgs& G, float* beauty,
+                             uint32_t* samples, uint32_t* pathcount);
 // Per-path radiance (spp x npix x 3, sample-major, output index order) and
 // vertex counts of the samples er_render makes with opts, into device
 // buffers (render.cu).  grad_wave: size the wave buffers for the gradient

@@ -332,7 +332,9 @@ __device__ __forceinline__ void grad_prev_vertex(const WaveView& w, const GradAr
 constexpr int kShadeMinBlocks = ER_SHADE_MIN_BLOCKS;
 constexpr int kShadeGradMinBlocks = ER_SHADE_GRAD_MIN_BLOCKS;
 
-template <bool BATCH, bool GRAD = false>
+// EVAL: the detached estimator of er_render_replay, BRDF values and
+// environment radiance from G's evaluation parameters.
+template <bool BATCH, bool GRAD = false, bool EVAL = false>
 __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlocks)
     k_shade(DevScene S0, WaveView w, WaveParams P0, int32_t bounce, BatchView B, GradArgs G) {
   const int32_t qin = bounce & 1;
@@ -384,7 +386,8 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
       if (slot < 0) {
         // kernel.cu:414-419: environment on escape, no MIS weight
         int64_t te = 0;
-        f3 e = escape_radiance(S, d, GRAD ? &te : nullptr);
+        f3 e = escape_radiance(S, d, (GRAD || EVAL) ? &te : nullptr);
+        if (EVAL && G.eval_env) e = mk(G.eval_env[3 * te], G.eval_env[3 * te + 1], G.eval_env[3 * te + 2]);
         if (GRAD) {
           const float4 dl4 = w.g_dl[p];
           float ge[3] = {dl4.x * thr.x, dl4.y * thr.y, dl4.z * thr.z};
@@ -399,6 +402,7 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         VertexShade V;
         shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
+        if (EVAL) eval_vertex(S, G.eval_mat, G.eval_env, d, V);
         if (GRAD) {
           const float4 dl4 = w.g_dl[p], lt = w.g_lt[p];
           vertex_grad_coeffs(S, V, thr, mk(dl4.x, dl4.y, dl4.z), mk(lt.x, lt.y, lt.z), mk(L.x, L.y, L.z),
@@ -733,6 +737,10 @@ er_status ensure_film(er_scene* s, bool aov, bool fp64, bool clear) {
     k_film_clear<<<(npix + 255) / 256, 256, 0, s->stream>>>(F, npix);
     ER_CUDA(cudaGetLastError());
   }
+  // the FP64 sums hold the whole film only if every render into it since
+  // the last clear accumulated them
+  if (!fp64) F.sum_valid = false;
+  else if (clear) F.sum_valid = true;
   return ER_OK;
 }
 
@@ -743,8 +751,10 @@ er_status copy_out(er_scene* s, bool dev, void* dst, const void* src, size_t byt
 }
 
 // Runs the waves of one call.  dump_rad != null: single wave, per-path dump.
+// eval != null: the shade stage takes its evaluation parameters (the
+// detached estimator of er_render_replay).
 er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* dump_b, int64_t* launches,
-              bool grad_wave = false) {
+              bool grad_wave = false, const GradArgs* eval = nullptr) {
   const int32_t W = s->camera.x_res, H = s->camera.y_res;
   const int32_t npix = W * H;
   const bool aov = o->flags & ER_RENDER_AOV;
@@ -823,7 +833,8 @@ er_status run(er_scene* s, const er_render_opts* o, float* dump_rad, int32_t* du
       }
       if ((st = mark(ER_STAGE_TRACE)) != ER_OK) return st;
       if (b == max_depth) break;
-      k_shade<false><<<g_shade, 128, 0, strm>>>(s->dev, w, P, b, NB, GradArgs{});
+      if (eval) k_shade<false, false, true><<<g_shade, 128, 0, strm>>>(s->dev, w, P, b, NB, *eval);
+      else k_shade<false><<<g_shade, 128, 0, strm>>>(s->dev, w, P, b, NB, GradArgs{});
       if ((st = mark(ER_STAGE_SHADE)) != ER_OK) return st;
     }
     if (dump_rad) {
@@ -1099,6 +1110,24 @@ er_status film_read_async(er_scene* s, uint32_t flags, float* beauty, float* nor
 }
 
 }  // namespace
+
+er_status render_eval_device(er_scene* s, const er_render_opts* o, const GradArgs& G, float* beauty,
+                             uint32_t* samples, uint32_t* pathcount) {
+  const bool fp64 = o->flags & ER_RENDER_ACCUM_FP64;
+  er_status st = ensure_film(s, false, fp64, true);
+  if (st != ER_OK) return st;
+  er_render_opts oo = *o;
+  oo.flags &= ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64;
+  int64_t launches = 0;
+  const bool eval = G.eval_mat || G.eval_env;  // without either: er_render's own shade stage
+  if ((st = run(s, &oo, nullptr, nullptr, &launches, false, eval ? &G : nullptr)) != ER_OK) return st;
+  if ((st = film_read_async(s, o->flags & ER_RENDER_DEVICE_OUT, beauty, nullptr, nullptr, nullptr, samples,
+                            pathcount)) != ER_OK)
+    return st;
+  ER_CUDA(cudaStreamSynchronize(s->stream));
+  return check_device_error(s);
+}
+
 }  // namespace er
 
 extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, float* normal, float* tangent,
@@ -1107,6 +1136,23 @@ extern "C" er_status er_film_read(er_scene* s, uint32_t flags, float* beauty, fl
     if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
     er_status st = film_read_async(s, flags, beauty, normal, tangent, bitangent, samples, pathcount);
     if (st != ER_OK) return st;
+    ER_CUDA(cudaStreamSynchronize(s->stream));
+    return ER_OK;
+  });
+}
+
+extern "C" er_status er_film_read_sums(er_scene* s, uint32_t flags, double* sums, uint32_t* samples) {
+  return guarded("er_film_read_sums", [&]() -> er_status {
+    if (!s) return fail(ER_ERR_INVALID_ARG, "scene is NULL");
+    const Film& F = s->film;
+    if (!F.beauty || !F.sum || !F.sum_valid)
+      return fail(ER_ERR_INVALID_ARG, "the film holds no FP64 sums (render it with ER_RENDER_ACCUM_FP64)");
+    ER_CUDA(cudaSetDevice(s->device));
+    const bool dev = flags & ER_RENDER_DEVICE_OUT;
+    const size_t np = (size_t)F.w * F.h;
+    er_status st;
+    if ((st = copy_out(s, dev, sums, F.sum, np * 3 * sizeof(double))) != ER_OK) return st;
+    if ((st = copy_out(s, dev, samples, F.samples, np * sizeof(uint32_t))) != ER_OK) return st;
     ER_CUDA(cudaStreamSynchronize(s->stream));
     return ER_OK;
   });

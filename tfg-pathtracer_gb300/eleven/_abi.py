@@ -180,7 +180,7 @@ EXPORTED = [
     "er_batch_create", "er_batch_set_jobs", "er_batch_render", "er_batch_read",
     "er_batch_autotune", "er_batch_info", "er_batch_free",
     "er_trace_closest", "er_encode_ldr", "er_write_image", "er_postprocess", "er_compute_tangents",
-    "er_scene_folder_read", "er_folder_desc", "er_folder_free", "er_device_bandwidth",
+    "er_scene_folder_read", "er_folder_desc", "er_folder_free", "er_device_bandwidth", "er_film_read_sums",
 ]
 
 ER_BW_L2_READ, ER_BW_HBM_COPY = 0, 1

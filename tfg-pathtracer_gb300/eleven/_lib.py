@@ -67,6 +67,8 @@ def load(build_if_missing=True):
     L.er_film_read.restype = A.er_status
     L.er_film_read.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p]
+    L.er_film_read_sums.restype = A.er_status
+    L.er_film_read_sums.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
     L.er_snapshot.restype = A.er_status
     L.er_snapshot.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.er_env_distribution.restype = A.er_status
@@ -314,6 +316,15 @@ class Scene:
         samples = np.zeros(H * W, np.uint32)
         check(load().er_snapshot(self.h, _p(beauty), _p(samples)), "er_snapshot")
         return beauty, samples
+
+    def read_sums(self):
+        """FP64 per-pixel sums ((H*W, 3) float64) and sample counts of the
+        film of an ER_RENDER_ACCUM_FP64 render (er_film_read_sums)."""
+        W, H = self.resolution
+        sums = np.zeros((H * W, 3), np.float64)
+        samples = np.zeros(H * W, np.uint32)
+        check(load().er_film_read_sums(self.h, 0, _p(sums), _p(samples)), "er_film_read_sums")
+        return sums, samples
 
     def render_paths(self, spp, max_depth=5, seed=0, sample_begin=0):
         W, H = self.resolution

@@ -66,3 +66,26 @@ def reduce_film(beauty, samples, group=None):
     if is_t:
         return out, cnt
     return out.numpy(), cnt.numpy().astype(np.uint32)
+
+
+def reduce_sums(sums, samples, group=None):
+    """All-reduce of one rank's exact film (the FP64 per-pixel sums and
+    sample counts of an ER_RENDER_ACCUM_FP64 render, er_film_read_sums):
+    every rank gets the summed sums and counts, and the merged beauty (the
+    FP64 means rounded once to float32, alpha 1).  Unlike reduce_film no
+    rank's mean is rounded before the merge, so the result equals one
+    process rendering every sample in FP64 up to the order of the additions."""
+    import torch
+    import torch.distributed as dist
+    is_t = torch.is_tensor(sums)
+    sm = sums.to(torch.float64) if is_t else torch.from_numpy(np.ascontiguousarray(sums, np.float64))
+    s64 = (samples if torch.is_tensor(samples) else torch.from_numpy(np.ascontiguousarray(samples).astype(np.int64)))
+    s64 = s64.to(torch.float64)
+    dist.all_reduce(sm, group=group)
+    dist.all_reduce(s64, group=group)
+    beauty = torch.ones((sm.shape[0], 4), dtype=torch.float32, device=sm.device)
+    beauty[:, :3] = torch.where(s64[:, None] > 0, sm / s64.clamp(min=1)[:, None], torch.zeros_like(sm)).float()
+    cnt = s64.round().to(torch.int64)
+    if is_t:
+        return sm, cnt, beauty
+    return sm.numpy(), cnt.numpy().astype(np.uint32), beauty.numpy()
