@@ -365,11 +365,11 @@ def run_reference(args):
     W, H = arrays.camera["x_res"], arrays.camera["y_res"]
     orc = O.OrcScene(arrays)
     cores = os.cpu_count() or 1
-    # size one step to ~1.5 s of host work
+    # size one step to ~0.5 s of host work (the default 128 steps then take about a minute)
     t = time.perf_counter()
     orc.render(spp=1, max_depth=max_depth, pixel_stride=4096)
     rate = ((W * H + 4095) // 4096) / max(time.perf_counter() - t, 1e-3)
-    stride = max(1, int(W * H / max(1.0, rate * 1.5)))
+    stride = max(1, int(W * H / max(1.0, rate * 0.5)))
     n = (W * H + stride - 1) // stride
     for i in range(args.warmup):
         orc.render(spp=1, max_depth=max_depth, sample_begin=i, pixel_stride=stride)
