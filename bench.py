@@ -633,7 +633,7 @@ def measure_adjoint(steps, warmup, fd_params):
     forward render (er_render) plus one er_backward; value = full-gradient
     evaluations per second.  The check: central differences (h = 1e-3,
     common random numbers) of the detached estimator on --fd-params random
-    parameters, at 16 spp."""
+    differentiable parameters, at 256 spp, from the films' FP64 sums."""
     from eleven import _abi as A
     from eleven import _lib, scenes
     spp, depth = 64, 6
@@ -670,18 +670,26 @@ def measure_adjoint(steps, warmup, fd_params):
     s.render_replay(spp, max_depth=depth, seed=7)
     replay_ms = (time.perf_counter() - t0) * 1e3
 
-    # finite-difference check of the detached estimator at 16 spp
-    fspp, h = 16, 1e-3
+    # finite-difference check of the detached estimator (the check of
+    # tests/test_gpu_full_configs.py at 256 instead of 4096 spp): central
+    # differences of the films' exact FP64 sums on half albedo / roughness
+    # and half environment parameters (metallic, drawn from {0, 1}, sits on
+    # the estimator's kinks)
+    fspp, h = 256, 1e-3
     out = s.render(fspp, max_depth=depth, seed=5)
     d = np.zeros_like(out["beauty"])
     d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
     gm, ge, _ = s.backward(fspp, d, out["samples"], max_depth=depth, seed=5)
     g = np.concatenate([gm.ravel(), ge.ravel()])
     rng = np.random.default_rng(32)
-    idx = rng.choice(n_params, fd_params, replace=False)
+    smooth = np.nonzero(np.arange(m0.size) % 5 != 4)[0]
+    half = fd_params // 2
+    idx = list(rng.choice(smooth, half, replace=False)) + list(m0.size + rng.choice(e0.size, fd_params - half,
+                                                                                        replace=False))
 
-    def loss(img):
-        dd = img[:, :3].astype(np.float64) - T[:, :3].astype(np.float64)
+    def loss_exact():
+        sums, n = s.read_sums()
+        dd = sums / np.maximum(n, 1)[:, None] - T[:, :3].astype(np.float64)
         return float((dd * dd).sum())
 
     gmax = float(np.abs(g).max())
@@ -694,9 +702,10 @@ def measure_adjoint(steps, warmup, fd_params):
                 m.ravel()[k] += sign * h
             else:
                 e.ravel()[k - m0.size] += sign * h
-            vals.append(loss(s.render_replay(fspp, max_depth=depth, seed=5, materials=m, env=e)["beauty"]))
+            s.render_replay(fspp, max_depth=depth, seed=5, materials=m, env=e, flags=A.ER_RENDER_ACCUM_FP64)
+            vals.append(loss_exact())
         fd = (vals[0] - vals[1]) / (2 * h)
-        if max(abs(fd), abs(g[k])) < 1e-4 * gmax:
+        if max(abs(fd), abs(g[k])) < 1e-7 * gmax:
             skipped += 1
             continue
         errs.append(abs(fd - g[k]) / max(abs(fd), abs(g[k])))
@@ -714,7 +723,8 @@ def measure_adjoint(steps, warmup, fd_params):
         "fd_check": {"params": int(fd_params), "checked": len(errs), "negligible": skipped,
                      "max_rel_err": round(float(max(errs)) if errs else 0.0, 6),
                      "median_rel_err": round(float(np.median(errs)) if errs else 0.0, 6),
-                     "h": h, "spp": fspp, "estimator": "detached sampling (er_render_replay)"},
+                     "h": h, "spp": fspp, "params_from": "albedo, roughness, environment texels",
+                     "estimator": "detached sampling (er_render_replay), FP64 film sums"},
         "gpu_launches": 2,
     }
     if clk:

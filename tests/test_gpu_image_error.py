@@ -63,7 +63,7 @@ def test_image_error_against_fp64_oracle(c1):
     }
     print("\nimage error vs FP64 oracle:", out)
     assert cnt.min() > 4000
-    assert out["matched_256spp_rel_rmse"] < 0.05
+    assert out["matched_256spp_rel_rmse"] < 0.03  # measured 0.021
     # the GPU image is as far from the converged render as the FP64
     # evaluation of the same samples is
     assert out["gpu256_vs_fp64_4096_rel_rmse"] < 1.2 * out["fp64_256_vs_fp64_4096_rel_rmse"] + 1e-3
