@@ -56,6 +56,8 @@ er_status check_replay_opts(er_scene* s, const er_render_opts* o) {
   if (!s || !o) return fail(ER_ERR_INVALID_ARG, "NULL argument");
   if (o->spp < 0 || o->sample_begin < 0 || o->max_depth < 0 || o->max_depth > 64)
     return fail(ER_ERR_INVALID_ARG, "render options out of range");
+  if ((int64_t)o->sample_begin + o->spp > INT32_MAX)
+    return fail(ER_ERR_INVALID_ARG, "sample_begin + spp exceeds INT32_MAX");
   if (o->flags & ~(uint32_t)(ER_RENDER_DEVICE_OUT | ER_RENDER_ENV_ALIAS | ER_RENDER_ACCUM_FP64))
     return fail(ER_ERR_INVALID_ARG, "only ER_RENDER_DEVICE_OUT, ER_RENDER_ENV_ALIAS and ER_RENDER_ACCUM_FP64 apply here");
   ER_CUDA(cudaSetDevice(s->device));
