@@ -97,4 +97,11 @@ def test_noalloc_rejects_oversized_images_and_flags():
     o = A.er_render_opts(1, 0, 4, 0, 0, A.ER_RENDER_AOV, 0)
     st = L.er_render_noalloc(scene.h, C.byref(o), C.c_void_p(16), C.c_void_p(16), C.c_void_p(16))
     assert st == A.ER_ERR_INVALID_ARG
+    # counters that are not 4-byte aligned are refused before any launch
+    # (the pointers are never dereferenced)
+    o = A.er_render_opts(1, 0, 4, 0, 0, 0, 0)
+    for smp, pc in ((18, 16), (16, 18)):
+        st = L.er_render_noalloc(scene.h, C.byref(o), C.c_void_p(16), C.c_void_p(smp), C.c_void_p(pc))
+        assert st == A.ER_ERR_INVALID_ARG
+        assert b"4-byte aligned" in L.er_last_error()
     scene.close()
