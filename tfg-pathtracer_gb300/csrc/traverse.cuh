@@ -40,6 +40,9 @@ constexpr int kTravMinBlocks = ER_TRAV_MIN_BLOCKS;  // blocks of 128 per SM the 
 constexpr int kSmemStack = ER_SMEM_STACK;   // stack entries per lane in shared memory
 constexpr int kLocalStack = 96 - kSmemStack;  // the rest in local memory
 constexpr int kMaxStack = kSmemStack + kLocalStack;
+#ifndef ER_Q8_FOLD
+#define ER_Q8_FOLD 1  // 8-bit nodes: plane decode folded into the slab fma
+#endif
 
 struct TravStats {
   uint32_t nodes, boxes, tris;
@@ -88,6 +91,13 @@ __device__ __forceinline__ f3 ref_position(f3 o, f3 d, float t, float u, float v
 // operations instead of a shift, a mask and an integer conversion.
 __device__ __forceinline__ float byte_of(uint32_t w, int c) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)c)) - 8388608.0f;
+}
+// Byte c of w placed in mantissa bits 8..15 of 2^23: the float 2^23 + 256 q,
+// exactly, from one byte permute.  Times a slab factor pre-scaled by 2^-8 it
+// is 2^15 A + q A; the constant 2^15 A goes into the node's bias once, so a
+// plane costs the permute and one fma.
+__device__ __forceinline__ float byte_hi(uint32_t w, int c) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7404u + ((uint32_t)c << 4)));
 }
 // Decoded Q8 plane origin + q * scale: q * scale is exact (q <= 255, the
 // scale a power of two), so the fused form rounds like the sum.
@@ -270,6 +280,32 @@ struct Traverser {
       // builder checked against the FP32 box.  An s inv that overflows
       // (node extents beyond 2^35) takes the plain decode.
       const float Ax = sx * inv.x, Ay = sy * inv.y, Az = sz * inv.z;
+#if ER_Q8_FOLD
+      // Folded form: t = fma(2^23 + 256 q, A 2^-8, B - 2^15 A) with the
+      // bias B - 2^15 A rounded down for near planes and up for far planes.
+      // Its exact value lies on the outer side of q A + B, and rounding is
+      // monotone, so every slab distance is at least as far out as the
+      // unfolded form's (a widening below one ulp of 2^15 A, 2^-8 of a
+      // quantisation step).  A 2^-8 and 2^15 A are exact while 2^-118 <=
+      // |A| < 2^112; other nodes take the unfolded form.
+      const float amax = max3f(fabsf(Ax), fabsf(Ay), fabsf(Az)), amin = min3f(fabsf(Ax), fabsf(Ay), fabsf(Az));
+      if (amax < 0x1p112f && amin >= 0x1p-118f) {
+        const float ax = Ax * 0x1p-8f, ay = Ay * 0x1p-8f, az = Az * 0x1p-8f;
+        const float cx = Ax * -0x1p15f, cy = Ay * -0x1p15f, cz = Az * -0x1p15f;
+        const float Bnx = __fadd_rd(fmaf(ox, inv.x, bnear.x), cx), Bfx = __fadd_ru(fmaf(ox, inv.x, bfar.x), cx);
+        const float Bny = __fadd_rd(fmaf(oy, inv.y, bnear.y), cy), Bfy = __fadd_ru(fmaf(oy, inv.y, bfar.y), cy);
+        const float Bnz = __fadd_rd(fmaf(oz, inv.z, bnear.z), cz), Bfz = __fadd_ru(fmaf(oz, inv.z, bfar.z), cz);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          tnx[k] = fmaf(byte_hi(qnx, k), ax, Bnx);
+          tfx[k] = fmaf(byte_hi(qfx, k), ax, Bfx);
+          tny[k] = fmaf(byte_hi(qny, k), ay, Bny);
+          tfy[k] = fmaf(byte_hi(qfy, k), ay, Bfy);
+          tnz[k] = fmaf(byte_hi(qnz, k), az, Bnz);
+          tfz[k] = fmaf(byte_hi(qfz, k), az, Bfz);
+        }
+      } else
+#endif
       if (fabsf(Ax) < INFINITY && fabsf(Ay) < INFINITY && fabsf(Az) < INFINITY) {
         const float Bnx = fmaf(ox, inv.x, bnear.x), Bfx = fmaf(ox, inv.x, bfar.x);
         const float Bny = fmaf(oy, inv.y, bnear.y), Bfy = fmaf(oy, inv.y, bfar.y);
