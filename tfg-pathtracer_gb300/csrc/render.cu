@@ -401,7 +401,8 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
         int32_t pix = path_pixel(P, local % P.npix), s = local / P.npix;
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         VertexShade V;
-        shade_vertex(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z, slot, V);
+        shade_vertex<BATCH>(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z,
+                            slot, V);
         if (EVAL) eval_vertex(S, G.eval_mat, G.eval_env, d, V);
         if (GRAD) {
           const float4 dl4 = w.g_dl[p], lt = w.g_lt[p];

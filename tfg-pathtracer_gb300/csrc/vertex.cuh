@@ -82,6 +82,7 @@ struct VertexShade {
 
 // Shades the closest hit (t, u, v, slot) of ray (o, d) at vertex `bounce`
 // of the sample with output index idx and sample number `sample`.
+template <bool EVAL_LOOP = false>
 __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, uint32_t k0, uint32_t k1, uint32_t idx,
                                              uint32_t sample, int32_t bounce, f3 o, f3 d, float t, float u, float v,
                                              int32_t slot, VertexShade& V) {
@@ -152,8 +153,39 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   const DisneyCtx& C = V.C;
   f3 dir = disney_sample(hd, C, u01(rn.x), u01(rn.y), u01(rn.z));
   float r1 = u01(rn.w);
+  f3 dH = -normalized(reverse_spherical(iu, iv));
+  // EVAL_LOOP: the point light's direction first, so that the BRDF is
+  // evaluated for the three directions by one copy of its code (a loop, not
+  // unrolled), for a smaller hot loop in the instruction cache; the values
+  // are the same either way.  Measured per workload (same call): the 64-job
+  // batch of small scenes 3.9 % faster with the loop, the 1080p textured
+  // scene 6 % slower in the shade stage (more spilling), so the batch
+  // kernels take the loop and the plain kernels the three inlined calls.
+  int32_t li = 0;
+  f3 toL = mk1(0.f), dP = mk1(0.f);
+  auto light_dir = [&]() {
+    li = min(__float2int_rz((float)S.n_lights * r1), S.n_lights - 1);
+    const er_point_light& Lq = S.lights[li];
+    toL = xsub(mk(Lq.position[0], Lq.position[1], Lq.position[2]), pos);
+    dP = normalized(toL);
+  };
+  if (EVAL_LOOP && S.n_lights > 0) light_dir();
+  f3 f, fH, fP = mk1(0.f);
+  if (EVAL_LOOP) {
+    const int n_eval = S.n_lights > 0 ? 3 : 2;
+#pragma unroll 1
+    for (int k = 0; k < n_eval; k++) {
+      const f3 L = k == 0 ? dir : (k == 1 ? dH : dP);
+      const f3 e = disney_eval(hd, C, L);
+      if (k == 0) f = e;
+      else if (k == 1) fH = e;
+      else fP = e;
+    }
+  } else {
+    f = disney_eval(hd, C, dir);
+    fH = disney_eval(hd, C, dH);
+  }
   // shade, kernel.cu:339-358
-  f3 f = disney_eval(hd, C, dir);
   float brdfPdf = disney_pdf(C, dir);
   float ndl = fabsf(dot(dir, hd.normal));
   V.dir = dir;
@@ -162,9 +194,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   V.ndl = ndl;
   // HDRI NEE, kernel.cu:234-257 (the pdf is defined even when blocked);
   // the texel (iu, iv) and its value eH were fetched above
-  f3 dH = -normalized(reverse_spherical(iu, iv));
   float hdriPdf = hdri_pdf(S, eH, ey);
-  f3 fH = disney_eval(hd, C, dH);
   float cosH = fabsf(dot(dH, hd.normal));
   f3 hdriC = (fH * cosH) * eH / hdriPdf;
   V.dH = dH;
@@ -183,13 +213,12 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   V.dist = V.cosP = 0.f;
   if (S.n_lights > 0) {
     pointPdf = (float)S.n_lights / (2.0f * ER_PI);
-    int32_t li = min(__float2int_rz((float)S.n_lights * r1), S.n_lights - 1);
+    if (!EVAL_LOOP) {
+      light_dir();
+      fP = disney_eval(hd, C, dP);
+    }
     const er_point_light& Lp = S.lights[li];
-    f3 lp = mk(Lp.position[0], Lp.position[1], Lp.position[2]);
-    f3 toL = xsub(lp, pos);
-    f3 dP = normalized(toL);
     float dist = xlen(toL);
-    f3 fP = disney_eval(hd, C, dP);
     f3 plv = mk(Lp.radiance[0], Lp.radiance[1], Lp.radiance[2]) / (dist * dist);
     float cosP = fabsf(dot(dP, hd.normal));
     pointC = (plv * fP) * cosP / pointPdf;
