@@ -652,7 +652,7 @@ def measure_adjoint(steps, warmup, fd_params):
         d = np.zeros_like(out["beauty"])
         d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
         gm, ge, st = s.backward(spp, d, out["samples"], max_depth=depth, seed=seed)
-        return out["stats"].ms, st.ms, gm, ge
+        return out["stats"].ms, st.ms, gm, ge, int(out["stats"].kernel_launches) + int(st.kernel_launches)
 
     for w in range(max(1, warmup)):
         step(1000 + w)
@@ -725,7 +725,7 @@ def measure_adjoint(steps, warmup, fd_params):
                      "median_rel_err": round(float(np.median(errs)) if errs else 0.0, 6),
                      "h": h, "spp": fspp, "params_from": "albedo, roughness, environment texels",
                      "estimator": "detached sampling (er_render_replay), FP64 film sums"},
-        "gpu_launches": 2,
+        "gpu_launches": int(np.median([r[4] for r in res])),  # per step: forward + backward
     }
     if clk:
         line["clocks"] = clk

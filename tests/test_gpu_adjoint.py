@@ -191,7 +191,13 @@ def test_kept_paths_give_the_same_gradient(small):
         d = np.zeros_like(out["beauty"])
         d[:, :3] = 2.0 * (out["beauty"][:, :3] - T[:, :3])
         bs = seed if other_seed is None else other_seed
-        gm, ge, _ = s.backward(SPP, d, out["samples"], max_depth=DEPTH, seed=bs)
+        gm, ge, st = s.backward(SPP, d, out["samples"], max_depth=DEPTH, seed=bs)
+        # launches: per gradient wave raygen, DEPTH + 1 traces, DEPTH shades,
+        # the resolve; without kept radiance also the forward's own waves
+        # (raygen, traces, shades, the per-path dump)
+        waves = 2  # 16 spp at 48x40: waves of 8 samples
+        grad = waves * (2 * DEPTH + 3)
+        assert st.kernel_launches == (grad if keep else grad + waves * (2 * DEPTH + 3)), st.kernel_launches
         return gm, ge, d, out["samples"]
 
     def close(a, b):

@@ -276,10 +276,11 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
     float* d_rad = kept ? s->kp_rad : s->bw_rad;
     int32_t* d_b = s->bw_b;
     ER_CUDA(cudaEventRecord(s->ev0, s->stream));
+    int64_t launches = 0;
     if (npaths > 0) {
       er_render_opts oo = *o;
       oo.flags &= ER_RENDER_ENV_ALIAS;
-      if (!kept && (st = render_paths_device(s, &oo, d_rad, d_b, true)) != ER_OK) return st;
+      if (!kept && (st = render_paths_device(s, &oo, d_rad, d_b, true, &launches)) != ER_OK) return st;
       GradArgs G;
       G.rad = d_rad;
       G.d_beauty = A.d_beauty;
@@ -287,7 +288,7 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
       G.g_mat = A.g_mat;
       G.g_env = A.g_env;
       G.sample0 = o->sample_begin;
-      if ((st = render_backward_device(s, &oo, G)) != ER_OK) return st;
+      if ((st = render_backward_device(s, &oo, G, &launches)) != ER_OK) return st;
     }
     ER_CUDA(cudaEventRecord(s->ev1, s->stream));
     if (!dev) {
@@ -307,7 +308,7 @@ extern "C" er_status er_backward(er_scene* s, const er_render_opts* o, const flo
       cudaEventElapsedTime(&ms, s->ev0, s->ev1);
       stats->ms = ms;
       stats->samples = (int64_t)o->spp * (int64_t)np;
-      stats->kernel_launches = npaths > 0 ? 2 * A.P.max_depth + 4 : 0;
+      stats->kernel_launches = launches;
     }
     return ER_OK;
   });

@@ -371,8 +371,8 @@ struct GradArgs {
   int32_t sample0 = 0;
 };
 // Runs the samples of opts through the wavefront with the gradient variant
-// of the shade stage (render.cu).
-er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G);
+// of the shade stage (render.cu); adds its kernel launches to *launches.
+er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G, int64_t* launches);
 // The detached estimator (er_render_replay): the samples of opts through the
 // wavefront with BRDF values and environment radiance from the evaluation
 // parameters in G (device arrays), into the scene's film; outputs as
@@ -382,9 +382,10 @@ er_status render_eval_device(er_scene* s, const er_render_opts* o, const GradArg
 // Per-path radiance (spp x npix x 3, sample-major, output index order) and
 // vertex counts of the samples er_render makes with opts, into device
 // buffers (render.cu).  grad_wave: size the wave buffers for the gradient
-// wavefront that follows, so that it reuses them.
+// wavefront that follows, so that it reuses them.  launches != null: set to
+// the kernel launches it made.
 er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b,
-                              bool grad_wave = false);
+                              bool grad_wave = false, int64_t* launches = nullptr);
 // Wavefront buffers for `cap` paths (render.cu); stats = device ray counters.
 er_status wave_create(int64_t cap, unsigned long long* stats, Wave** out);
 void wave_destroy(Wave* w);

@@ -925,16 +925,17 @@ void free_film(er_scene* s) {
   F = Film();
 }
 
-er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b, bool grad_wave) {
+er_status render_paths_device(er_scene* s, const er_render_opts* o, float* d_rad, int32_t* d_b, bool grad_wave,
+                              int64_t* launches) {
   er_render_opts oo = *o;
   oo.flags &= ~(uint32_t)(ER_RENDER_AOV | ER_RENDER_SNAPSHOTS);
-  return run(s, &oo, d_rad, d_b, nullptr, grad_wave);
+  return run(s, &oo, d_rad, d_b, launches, grad_wave);
 }
 
 // The gradient wavefront: the same waves as run(), with the gradient
 // variants of raygen and shade and a final per-path resolve in place of the
 // accumulation.
-er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G) {
+er_status render_backward_device(er_scene* s, const er_render_opts* o, const GradArgs& G, int64_t* launches) {
   const int32_t W = s->camera.x_res, H = s->camera.y_res;
   const int32_t npix = W * H;
   const int32_t max_depth = o->max_depth > 0 ? o->max_depth : 5;
@@ -978,6 +979,7 @@ er_status render_backward_device(er_scene* s, const er_render_opts* o, const Gra
     }
     k_resolve_grad<<<(n + 255) / 256, 256, 0, strm>>>(w, n, G);
     ER_CUDA(cudaGetLastError());
+    *launches += 2 * max_depth + 3;  // raygen, max_depth + 1 traces, max_depth shades, resolve
   }
   if (two) {
     ER_CUDA(cudaEventRecord(s->ev_acc[0], s->stream2));
