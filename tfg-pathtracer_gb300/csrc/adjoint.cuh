@@ -212,21 +212,43 @@ __device__ __forceinline__ void vertex_grad_coeffs(const DevScene& S, const Vert
     const f3 uB = mk(wd.x * kB.x + r0.x, wd.y * kB.y + r0.y, wd.z * kB.z + r0.z);
     const f3 uH = mk(wd.x * kH.x, wd.y * kH.y, wd.z * kH.z);
     const f3 uP = mk(wd.x * kP.x, wd.y * kP.y, wd.z * kP.z);
-    const EvalGrad G = disney_eval_grad(V.hd, C, V.dir);
-    const EvalGrad GH = disney_eval_grad(V.hd, C, V.dH);
-    EvalGrad GP;
-    GP.dA[0] = GP.dA[1] = GP.dA[2] = GP.dM = GP.dR = mk1(0.f);
-    if (V.has_pt) GP = disney_eval_grad(V.hd, C, V.dP);
-    auto put = [&](int k, f3 g, f3 gh, f3 gp, float chain) {
-      k0[k] = chain * dot(uB, g);
-      kh[k] = chain * (dot(rH, g) + dot(uH, gh));
-      kp[k] = chain * (dot(rP, g) + dot(uP, gp));
+    // per parameter k, with g, gh, gp its BRDF derivative for the sampled,
+    // env and light directions:
+    //   k0 = chain * (uB . g), kh = chain * (rH . g + uH . gh),
+    //   kp = chain * (rP . g + uP . gp).
+    // The three derivative evaluations run in one loop (one copy of the
+    // code; this kernel is bound by instruction fetch), the sums formed in
+    // the same order as written out.
+    float s0[kParams], sh[kParams], sp[kParams];
+#pragma unroll 1
+    for (int j = 0; j < 3; j++) {
+      EvalGrad E;
+      E.dA[0] = E.dA[1] = E.dA[2] = E.dM = E.dR = mk1(0.f);
+      if (j < 2 || V.has_pt) E = disney_eval_grad(V.hd, C, j == 0 ? V.dir : (j == 1 ? V.dH : V.dP));
+#pragma unroll
+      for (int k = 0; k < kParams; k++) {
+        const f3 g = k < 3 ? E.dA[k] : (k == 3 ? E.dR : E.dM);
+        if (j == 0) {
+          s0[k] = dot(uB, g);
+          sh[k] = dot(rH, g);
+          sp[k] = dot(rP, g);
+        } else if (j == 1) {
+          sh[k] = sh[k] + dot(uH, g);
+        } else {
+          sp[k] = sp[k] + dot(uP, g);
+        }
+      }
+    }
+    auto put = [&](int k, float chain) {
+      k0[k] = chain * s0[k];
+      kh[k] = chain * sh[k];
+      kp[k] = chain * sp[k];
     };
     if (ca)
 #pragma unroll
-      for (int j = 0; j < 3; j++) put(j, G.dA[j], GH.dA[j], GP.dA[j], 1.0f);
-    if (dr) put(3, G.dR, GH.dR, GP.dR, 2.2f * powf(V.rough_in, 1.2f));
-    if (dm) put(4, G.dM, GH.dM, GP.dM, 2.2f * powf(V.metal_in, 1.2f));
+      for (int j = 0; j < 3; j++) put(j, 1.0f);
+    if (dr) put(3, 2.2f * powf(V.rough_in, 1.2f));
+    if (dm) put(4, 2.2f * powf(V.metal_in, 1.2f));
   }
   const float sH = V.cosH / V.hdriPdf * V.w1;
   out[0] = make_float4(k0[0], k0[1], k0[2], k0[3]);

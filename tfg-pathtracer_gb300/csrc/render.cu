@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(128, GRAD ? kShadeGradMinBlocks : kShadeMinBlo
         int32_t pix = path_pixel(P, local % P.npix), s = local / P.npix;
         uint32_t idx = (uint32_t)out_index(P, pix % P.W, pix / P.W);
         VertexShade V;
-        shade_vertex<BATCH>(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z,
+        shade_vertex<BATCH || GRAD>(S, P.flags, P.k0, P.k1, idx, (uint32_t)(P.sample_base + s), bounce, o, d, h.x, h.y, h.z,
                             slot, V);
         if (EVAL) eval_vertex(S, G.eval_mat, G.eval_env, d, V);
         if (GRAD) {

@@ -159,8 +159,9 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   // unrolled), for a smaller hot loop in the instruction cache; the values
   // are the same either way.  Measured per workload (same call): the 64-job
   // batch of small scenes 3.9 % faster with the loop, the 1080p textured
-  // scene 6 % slower in the shade stage (more spilling), so the batch
-  // kernels take the loop and the plain kernels the three inlined calls.
+  // scene 6 % slower in the shade stage (more spilling), so the batch and
+  // gradient kernels take the loop and the plain kernels the three inlined
+  // calls.
   int32_t li = 0;
   f3 toL = mk1(0.f), dP = mk1(0.f);
   auto light_dir = [&]() {
