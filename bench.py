@@ -522,7 +522,8 @@ def run_gpu(args):
                            if k in b}
         a = measure_adjoint(3, 1, args.fd_params)
         line["adjoint"] = {k: a[k] for k in ("metric", "value", "unit", "ms_per_step", "config", "forward_ms",
-                                             "backward_ms", "backward_msamples_per_s", "fd_check", "clocks")
+                                             "backward_ms", "backward_msamples_per_s", "fd_check", "gpu_launches",
+                                             "clocks")
                            if k in a}
     if rank == 0:
         print(json.dumps(line), flush=True)
