@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--config", default="c1", choices=["c1", "c0", "c2", "c4"])
     ap.add_argument("--fd-params", type=int, default=32, help="c4: parameters in the finite-difference check")
     ap.add_argument("--jobs", type=int, default=64, help="c2: number of batch jobs")
+    ap.add_argument("--steady", action="store_true",
+                    help="c2: also time every job alone at full-size waves (its steady-state cost per sample) "
+                         "and print the sum beside the plain and batched times")
     ap.add_argument("--bvh", default="fp32", choices=["fp32", "q8"])
     ap.add_argument("--max-leaf", type=int, default=0, help="triangles per BVH leaf (0 = library default)")
     ap.add_argument("--builder", default="host", choices=["host", "gpu"], help="BVH builder")
@@ -534,8 +537,41 @@ def run_gpu(args):
 
 def run_batch(args):
     line = measure_batch(args.jobs, args.steps, args.warmup)
+    if args.steady:
+        line["steady"] = measure_steady(args.jobs)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def measure_steady(n_jobs):
+    """The 64-job workload's cost if every job ran at the efficiency of a
+    large render of its own scene: each job alone with 4 full-size waves
+    (4 x floor(2^24 / pixels) samples per pixel), its time scaled to the
+    job's own sample count, summed over the jobs (FP32 and 8-bit nodes).
+    Batching removes small-job and launch losses; it cannot go below this
+    sum unless jobs gain from sharing waves."""
+    from eleven import _abi as A
+    from eleven import _lib, scenes
+    arrays, jobs = scenes.config2(n_jobs=n_jobs)
+    NO = A.ER_RENDER_NO_OUTPUT
+    tot = {"samples": 0, "fp32_ms": 0.0, "q8_ms": 0.0}
+    small = []
+    for a, j in zip(arrays, jobs):
+        npix = a.camera["x_res"] * a.camera["y_res"]
+        spp_s = 4 * max(1, (1 << 24) // npix)
+        samples = j["spp"] * npix
+        for fmt, key in ((A.ER_BVH_FP32, "fp32_ms"), (A.ER_BVH_Q8, "q8_ms")):
+            s = _lib.Scene(a, bvh_format=fmt)  # one scene at a time: full-size waves hold ~10 GB each
+            # the first render allocates the waves (inside its timed span): untimed
+            s.render(spp_s, max_depth=j["max_depth"], seed=j["seed"] + 2, flags=NO)
+            ms = s.render(spp_s, max_depth=j["max_depth"], seed=j["seed"] + 1, flags=NO)["stats"].ms
+            s.close()
+            tot[key] += ms * samples / (spp_s * npix)
+        tot["samples"] += samples
+    return {"what": "sum over jobs of each job's cost per sample alone at 4 full-size waves x its samples",
+            "fp32_ms": round(tot["fp32_ms"], 2), "q8_ms": round(tot["q8_ms"], 2),
+            "fp32_msamples_per_s": round(tot["samples"] / tot["fp32_ms"] / 1e3, 1),
+            "q8_msamples_per_s": round(tot["samples"] / tot["q8_ms"] / 1e3, 1)}
 
 
 def measure_batch(n_jobs, steps, warmup):
