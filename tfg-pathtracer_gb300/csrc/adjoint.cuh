@@ -247,8 +247,11 @@ __device__ __forceinline__ void vertex_grad_coeffs(const DevScene& S, const Vert
     if (ca)
 #pragma unroll
       for (int j = 0; j < 3; j++) put(j, 1.0f);
-    if (dr) put(3, 2.2f * powf(V.rough_in, 1.2f));
-    if (dm) put(4, 2.2f * powf(V.metal_in, 1.2f));
+    // d x^2.2 / dx = 2.2 x^1.2 = 2.2 x^2.2 / x, x^2.2 being the remapped
+    // value the vertex already holds (x > 0 here): no further powf in this
+    // instruction-fetch-bound kernel
+    if (dr) put(3, 2.2f * (V.hd.roughness / V.rough_in));
+    if (dm) put(4, 2.2f * (V.hd.metallic / V.metal_in));
   }
   const float sH = V.cosH / V.hdriPdf * V.w1;
   out[0] = make_float4(k0[0], k0[1], k0[2], k0[3]);

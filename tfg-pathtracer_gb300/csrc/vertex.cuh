@@ -137,8 +137,21 @@ __device__ __forceinline__ void shade_vertex(const DevScene& S, uint32_t flags, 
   }
   V.rough_in = rough;
   V.metal_in = metal;
-  hd.roughness = powf(rough, 2.2f);
-  hd.metallic = powf(metal, 2.2f);
+  if (EVAL_LOOP) {
+    // one copy of powf for both remaps (the pair rotated through a loop)
+    float pr = rough, pm = metal;
+#pragma unroll 1
+    for (int k = 0; k < 2; k++) {
+      const float r = powf(pr, 2.2f);
+      pr = pm;
+      pm = r;
+    }
+    hd.roughness = pr;
+    hd.metallic = pm;
+  } else {
+    hd.roughness = powf(rough, 2.2f);
+    hd.metallic = powf(metal, 2.2f);
+  }
   hd.clearcoatGloss = M.clearcoat_gloss;
   hd.clearcoat = M.clearcoat;
   hd.anisotropic = M.anisotropic;
