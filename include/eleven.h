@@ -394,7 +394,9 @@ er_status er_render_replay(er_scene* scene, const er_render_opts* opts, const fl
  * env w*h*3 floats.  The samples' radiance comes from the last er_render
  * when it ran with ER_RENDER_KEEP_PATHS and the same seed, sample range,
  * depth and env sampling, with no er_scene_set_params / set_camera since;
- * otherwise er_backward renders them again first. */
+ * otherwise er_backward renders them again first.  stats (may be NULL):
+ * ms = device time of the replay (and of the forward it renders again),
+ * samples, kernel_launches; the ray counters stay 0. */
 er_status er_backward(er_scene* scene, const er_render_opts* opts, const float* d_beauty, const uint32_t* samples,
                       float* grad_materials, float* grad_env, er_render_stats* stats);
 
